@@ -1,0 +1,177 @@
+/*
+ * mp_core.h -- C ABI of the GB300 REYES core (libmpcore.so).
+ *
+ * Drop-in for the reference's renderer boundary, the abstract Reyes::Renderer
+ * (src/Reyes/Renderer.h:29-45) and its OpenCL implementation RendererCL
+ * (src/Reyes/RendererCL.cpp:115-260).  Plain pointers and sizes only; every
+ * call returns an mp_status and never throws.  One context per host thread;
+ * all device work of a context runs on its CUDA stream.
+ */
+#ifndef MP_CORE_H
+#define MP_CORE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Error codes.  The reference signals errors with C++ exceptions
+ * (CL::Exception via OPENCL_ASSERT, src/CL/Exception.h) and assert(); here
+ * every entry point returns one of these and mp_last_error() gives the text. */
+typedef enum {
+    MP_OK = 0,
+    MP_ERR_INVALID_ARG = 1,  /* bad option, handle, size or pointer */
+    MP_ERR_OUT_OF_MEMORY = 2,
+    MP_ERR_OVERFLOW = 3,     /* a queue or output capacity was exceeded and could not grow */
+    MP_ERR_TIMEOUT = 4,      /* a bounded device wait gave up (no GPU hang) */
+    MP_ERR_CUDA = 5,         /* a CUDA runtime call failed */
+    MP_ERR_NOT_LOADED = 6,   /* draw of a handle with no loaded patches */
+    MP_ERR_STATE = 7         /* call out of order (e.g. draw before prepare) */
+} mp_status;
+
+/* src/Reyes/PatchType.h:6-9 */
+typedef enum { MP_BEZIER = 0, MP_GREGORY = 1 } mp_patch_type;
+
+/* Execution path of a frame. */
+typedef enum {
+    MP_PATH_PLAIN = 0,   /* per-pass: bound&split up to reyes_patches_per_pass, then dice,
+                            shade, sample with grids in device memory, host sync per pass */
+    MP_PATH_BATCHED = 1  /* one persistent launch per stage over all draws of the frame,
+                            replayed as a CUDA graph; no grids stored */
+} mp_path;
+
+/* Options, named as in the reference's reyes.options (values there are the
+ * defaults filled by mp_options_default). */
+typedef struct {
+    int32_t window_size[2];         /* framebuffer size; multiples of 8, at most 4096 */
+    int32_t reyes_patch_size;       /* dice grid: 8 or 16 quads per side */
+    float bound_n_split_limit;      /* pixels */
+    int32_t reyes_patches_per_pass; /* plain path pass size */
+    float cull_ribbon;              /* pixels */
+    int32_t max_split_depth;        /* at most 254 */
+    int32_t bound_sample_rate;      /* must be 3 (the CPU criterion samples 3x3) */
+    int32_t subpixel_bits;          /* fixed-point bits of pixel coordinates (1..8) */
+    int32_t framebuffer_tile_size;  /* must be 8 (the sample kernel's tile) */
+    int32_t backface_culling;
+    int32_t displacement;
+    float displacement_amplitude;   /* multiplies the hard-coded 0.04/0.02/0.01 */
+    float clear_color[4];
+    int32_t batch_views;            /* framebuffer layers (independent views) */
+    int32_t path;                   /* mp_path */
+    /* capacities (elements); 0 = automatic.  They grow on overflow. */
+    int64_t queue_capacity;         /* bound&split work items */
+    int64_t subpatch_capacity;      /* emitted sub-patches per frame */
+    int64_t spin_limit;             /* bounded-wait iterations before MP_ERR_TIMEOUT */
+} mp_options;
+
+/* The reference's Projection(fovy, near, viewport) (src/base/Projection.h:144). */
+typedef struct {
+    float fovy_deg;
+    float near_plane;
+    int32_t viewport[2];            /* must equal window_size */
+} mp_projection;
+
+typedef struct {
+    int64_t subpatches;             /* emitted sub-patches of the last frame */
+    int64_t micropolygons;          /* reyes_patch_size^2 * subpatches (src/base/Statistics.cpp:175) */
+    int64_t bounds;                 /* ranges bounded by bound&split */
+    int64_t passes;                 /* plain path passes */
+    int64_t fragments;              /* covered (micropolygon, pixel) pairs */
+    int64_t big_quads;              /* quads on the exact slow raster path */
+    double gpu_ms;                  /* device time of the last frame (CUDA events) */
+    /* per-stage device times of the last frame when stage timing is on
+     * (mp_set_stage_timing); stages: 0 clear+reset, 1 bound&split, 2 dice+raster
+     * (plain: dice), 3 exact slow raster, 4 resolve (plain: shade), 5 plain sample,
+     * 6 plain pass resolve, 7 plain host readback gaps */
+    double stage_ms[8];
+} mp_stats;
+
+typedef struct mp_ctx mp_ctx;
+
+/* Fills the reyes.options defaults. */
+void mp_options_default(mp_options* opts);
+
+/* Creates a context on the current CUDA device (replaces RendererCL::RendererCL,
+ * src/Reyes/RendererCL.cpp:21-106). */
+mp_status mp_create(const mp_options* opts, mp_ctx** out);
+void mp_destroy(mp_ctx* ctx);
+const char* mp_last_error(const mp_ctx* ctx);
+/* Uses `stream` (a cudaStream_t) for all further work; NULL restores the context's own. */
+mp_status mp_set_stream(mp_ctx* ctx, void* stream);
+
+/* Renderer::are_patches_loaded (Renderer.h:35, PatchIndex.cpp:50-53). */
+mp_status mp_are_patches_loaded(mp_ctx* ctx, uint64_t handle, int32_t* loaded);
+/* Renderer::load_patches (Renderer.h:36, PatchIndex.cpp:57-100): copies n_points xyz
+ * points (16 per Bezier, 20 per Gregory patch) to the device, widened to (x,y,z,1).
+ * handle is an opaque key chosen by the caller (the reference uses the mesh pointer). */
+mp_status mp_load_patches(mp_ctx* ctx, uint64_t handle, const float* xyz, size_t n_points, mp_patch_type type);
+/* Same, from device memory (float4 x,y,z,1 per point), no host copy. */
+mp_status mp_load_patches_device(mp_ctx* ctx, uint64_t handle, const void* dev_xyz1, size_t n_points,
+                                 mp_patch_type type);
+/* PatchIndex::delete_patches (PatchIndex.cpp:103-108). */
+mp_status mp_delete_patches(mp_ctx* ctx, uint64_t handle);
+
+/* Renderer::prepare (RendererCL.cpp:115-135): begins a frame (clear colour ^2.2,
+ * alpha 1000, depth 0x7fffffff). */
+mp_status mp_prepare(mp_ctx* ctx);
+/* Renderer::draw_patches (RendererCL.cpp:170-200): modelview is column-major
+ * (glm layout), colour the object colour.  Draws into framebuffer layer 0. */
+mp_status mp_draw_patches(mp_ctx* ctx, uint64_t handle, const float modelview[16], const mp_projection* proj,
+                          const float color[4]);
+/* Same, into framebuffer layer `view` (batched independent views). */
+mp_status mp_draw_patches_view(mp_ctx* ctx, uint64_t handle, const float modelview[16], const mp_projection* proj,
+                               const float color[4], int32_t view);
+/* Renderer::finish (RendererCL.cpp:138-154): completes the frame; the framebuffer
+ * is ready when this returns. */
+mp_status mp_finish(mp_ctx* ctx);
+/* Stage timing: when on, the batched frame runs its stages as separate
+ * launches with CUDA events between them instead of one graph replay, and
+ * mp_stats.stage_ms is filled (for profiling; the graph replay is faster). */
+mp_status mp_set_stage_timing(mp_ctx* ctx, int32_t on);
+/* Renderer::dump_trace (Renderer.h:43): per-stage device times of the last frame
+ * as `name@queue:queued:submit:start:end:id:` lines (src/CL/Device.cpp:275-289)
+ * into buf (NUL-terminated, truncated to cap). */
+mp_status mp_dump_trace(mp_ctx* ctx, char* buf, size_t cap);
+
+/* Headless framebuffer (replaces OGLSharedFramebuffer, src/Reyes/Framebuffer.cpp:75-144):
+ * tiled float4 colour and int32 depth, 8x8-pixel tiles, index
+ * (tx + ceil(W/8)*ty)*64 + lx + 8*ly (kernels/reyes.cl:37-45), one layer per view. */
+mp_status mp_framebuffer(mp_ctx* ctx, void** color_dev, void** depth_dev, int32_t* width, int32_t* height,
+                         int32_t* views);
+/* Copies layer `view` to host memory; linear != 0 converts to row-major (y up). */
+mp_status mp_read_framebuffer(mp_ctx* ctx, int32_t view, float* color_rgba, int32_t* depth, int32_t linear);
+
+/* Sub-patches of the last frame, for parity checks: count, then up to cap records
+ * (draw index, patch id, range min.x min.y max.x max.y).  Any pointer may be NULL. */
+mp_status mp_subpatches(mp_ctx* ctx, int64_t* count, int32_t* draw, int32_t* pid, float* range, int64_t cap);
+mp_status mp_stats_get(mp_ctx* ctx, mp_stats* stats);
+
+/* Dice grids of explicit sub-patches of the last frame's draw 0 mesh list
+ * (parity of the dicer): positions (float4), fixed-point pixels (int2), depth. */
+mp_status mp_dice_subpatches(mp_ctx* ctx, int32_t draw, int64_t n, const int32_t* pid, const float* range,
+                             float* pos, int32_t* pxl, float* depth);
+
+/* Adjoint of the last frame of layer `view`: grad_color (device, tiled float4 per
+ * pixel, dL/dcolour) -> dL/d control points of every draw whose gradient buffer is
+ * registered, and dL/d displacement amplitude (device float, accumulated).
+ * Visibility is the last frame's. */
+mp_status mp_set_grad_buffer(mp_ctx* ctx, int32_t draw, void* grad_dev);
+mp_status mp_backward(mp_ctx* ctx, int32_t view, const void* grad_color_dev, void* grad_amp_dev);
+/* Replaces the control points of a loaded handle in place from device memory (same count). */
+mp_status mp_update_patches_device(mp_ctx* ctx, uint64_t handle, const void* dev_xyz1);
+
+/* Inclusive prefix sum on the device (the decoupled look-back scan used by the
+ * plain path; the reference's CL::PrefixSum, src/CL/PrefixSum.cpp:33-80). */
+mp_status mp_inclusive_scan(mp_ctx* ctx, const int32_t* host_in, int32_t* host_out, int64_t n);
+
+/* 64-bit atomicMin throughput probe (atomics per second): pattern 0 uniform
+ * random slots, pattern 1 micropolygon-like locality. */
+mp_status mp_atomic_bench(mp_ctx* ctx, int64_t n_slots, int64_t n_ops, int32_t pattern, double* atomics_per_s);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MP_CORE_H */

@@ -1,0 +1,487 @@
+// Device-side math of the REYES core, shared by the bound-and-split,
+// dice/raster, resolve and adjoint kernels.
+//
+// Every floating-point operation whose rounding decides a result is written
+// with an explicit rounding intrinsic, and the whole library is compiled with
+// -fmad=false so nothing else is fused behind our back:
+//   * bound-and-split (src/Reyes/BoundNSplitCLCPU.cpp:249-336,
+//     src/base/Projection.cpp:57-106, src/base/Patch.cpp:107-210): no fused
+//     operations at all, so the emitted sub-patch set is bit-identical to the
+//     reference's CPU bound-and-split;
+//   * dice / shade / sample (kernels/dice.cl, kernels/reyes.cl,
+//     kernels/utility.h): the rounding choices allowed by the reference's
+//     -cl-mad-enable -cl-fast-relaxed-math build are fixed as
+//       R1 a*b + c is one fma; a*b + c*d = fma(c, d, a*b); a*b - c*d = fma(-c, d, a*b)
+//       R2 division and sqrt correctly rounded
+//       R3 max(x, 0) ignores NaN (fmaxf)
+//       R4 float->int truncates and saturates, NaN -> 0 (cvt.rzi.s32.f32)
+//       R5 int arithmetic wraps modulo 2^32
+//       R6 native_sin = mp_sinf (Cody-Waite reduction, Taylor polynomials)
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace mp {
+
+constexpr int kMaxPS = 16;
+
+// Per-draw constants (one draw = one mesh drawn with one modelview into one
+// framebuffer layer), resident in device memory.
+struct DrawDev {
+    const float4* cp;      // control points (x, y, z, 1), 16 or 20 per patch
+    float* grad_cp;        // adjoint output, xyz per control point (nullptr = none)
+    int n_patches;
+    int type;              // 0 Bezier, 1 Gregory
+    int view;              // framebuffer layer
+    int pad0;
+    float mv[16];          // column-major modelview (glm layout)
+    float proj[16];        // glm::perspective(fovy, aspect, near, 10000), column-major
+    float color[4];        // object colour
+    // Projection::bound (src/base/Projection.cpp:23-35)
+    float fx, fy, vpx, vpy;
+    float near_plane, cull_ribbon;
+    int vx, vy;
+};
+
+// Frame-wide constants.
+struct FrameDev {
+    int W, H;              // framebuffer size (all layers)
+    int PS;                // reyes_patch_size (8 or 16)
+    int shift;             // subpixel_bits
+    float limit;           // bound_n_split_limit
+    int max_depth;         // max_split_depth
+    int backface;          // backface_culling
+    int displacement;      // displacement on/off
+    float fdisp[3];        // 0.04, 0.02, 0.01 times the amplitude multiplier
+    float clear[4];        // clear colour (powf(c, 2.2), alpha 1000)
+    int gx, gy;            // 8-pixel tile grid of the output framebuffer
+    int n_draws;
+    int pad1;
+};
+
+// Depth|id key stored per pixel: (idepth << 32) | mp_id.  The clear key keeps
+// the reference's cleared depth 0x7fffffff (src/Reyes/RendererCL.cpp:123-126).
+constexpr unsigned long long kClearKey = 0x7fffffffffffffffULL;
+
+// ---------------------------------------------------------------------------
+// Bound-and-split arithmetic: plain IEEE, no fused operations.
+
+struct F3 { float x, y, z; };
+
+__device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float fdiv(float a, float b) { return __fdiv_rn(a, b); }
+// src/base/utility.h:86-94
+__device__ __forceinline__ float minimum(float a, float b) { return a < b ? a : b; }
+__device__ __forceinline__ float maximum(float a, float b) { return a > b ? a : b; }
+
+// src/base/Patch.cpp:107-113
+struct SplineW { float a, b, c, d; };
+__device__ __forceinline__ SplineW spline_weights(float t) {
+    float s = fsub(1.0f, t);
+    SplineW w;
+    w.a = fmul(fmul(s, s), s);
+    w.b = fmul(fmul(fmul(3.0f, s), s), t);
+    w.c = fmul(fmul(fmul(3.0f, s), t), t);
+    w.d = fmul(fmul(t, t), t);
+    return w;
+}
+__device__ __forceinline__ float spline1(const SplineW& w, float p0, float p1, float p2, float p3) {
+    return fadd(fadd(fadd(fmul(w.a, p0), fmul(w.b, p1)), fmul(w.c, p2)), fmul(w.d, p3));
+}
+__device__ __forceinline__ F3 spline3(const SplineW& w, const F3& p0, const F3& p1, const F3& p2,
+                                      const F3& p3) {
+    return F3{spline1(w, p0.x, p1.x, p2.x, p3.x), spline1(w, p0.y, p1.y, p2.y, p3.y),
+              spline1(w, p0.z, p1.z, p2.z, p3.z)};
+}
+__device__ __forceinline__ F3 ld3(const float4* p) {
+    float4 v = __ldg(p);
+    return F3{v.x, v.y, v.z};
+}
+
+// glm 0.9.9 mat4 * vec4(p, 1): (m0*x + m1*y) + (m2*z + m3*1), per component.
+__device__ __forceinline__ F3 mv_point(const float* m, const F3& p) {
+    F3 r;
+    r.x = fadd(fadd(fmul(m[0], p.x), fmul(m[4], p.y)), fadd(fmul(m[8], p.z), fmul(m[12], 1.0f)));
+    r.y = fadd(fadd(fmul(m[1], p.x), fmul(m[5], p.y)), fadd(fmul(m[9], p.z), fmul(m[13], 1.0f)));
+    r.z = fadd(fadd(fmul(m[2], p.x), fmul(m[6], p.y)), fadd(fmul(m[10], p.z), fmul(m[14], 1.0f)));
+    return r;
+}
+
+// glm::distance: sqrt((dx*dx + dy*dy) + dz*dz)
+__device__ __forceinline__ float distance3(const F3& a, const F3& b) {
+    float dx = fsub(b.x, a.x), dy = fsub(b.y, a.y), dz = fsub(b.z, a.z);
+    return __fsqrt_rn(fadd(fadd(fmul(dx, dx), fmul(dy, dy)), fmul(dz, dz)));
+}
+
+// Gregory patch (src/base/Patch.cpp:186-210), evaluated at (u, v) after the swap.
+__device__ __forceinline__ F3 blend3(float a, const F3& A, float b, const F3& B, float den) {
+    return F3{fdiv(fadd(fmul(a, A.x), fmul(b, B.x)), den), fdiv(fadd(fmul(a, A.y), fmul(b, B.y)), den),
+              fdiv(fadd(fmul(a, A.z), fmul(b, B.z)), den)};
+}
+__device__ __forceinline__ F3 eval_gregory_cpu(const float4* pd, float u_in, float v_in) {
+    float u = v_in, v = u_in;  // std::swap(u, v)
+    F3 F0 = blend3(u, ld3(pd + 12), v, ld3(pd + 16), fadd(u, v));
+    F3 F1 = blend3(fsub(1.0f, u), ld3(pd + 17), v, ld3(pd + 13), fadd(fsub(1.0f, u), v));
+    // F2 = ((1-u)*fm[2] + (1-v)*fp[2]) / (2-u-v): the CPU blend swaps the roles
+    // of fp and fm relative to the kernel version (kernels/utility.h:171)
+    F3 F2 = blend3(fsub(1.0f, u), ld3(pd + 18), fsub(1.0f, v), ld3(pd + 14), fsub(fsub(2.0f, u), v));
+    F3 F3v = blend3(u, ld3(pd + 19), fsub(1.0f, v), ld3(pd + 15), fsub(fadd(1.0f, u), v));
+    SplineW wu = spline_weights(u);
+    F3 P0 = spline3(wu, ld3(pd + 0), ld3(pd + 8), ld3(pd + 7), ld3(pd + 3));
+    F3 P1 = spline3(wu, ld3(pd + 4), F0, F3v, ld3(pd + 11));
+    F3 P2 = spline3(wu, ld3(pd + 9), F1, F2, ld3(pd + 6));
+    F3 P3 = spline3(wu, ld3(pd + 1), ld3(pd + 5), ld3(pd + 10), ld3(pd + 2));
+    return spline3(spline_weights(v), P0, P1, P2, P3);
+}
+
+// The range bound of src/Reyes/BoundNSplitCLCPU.cpp:249-336: 3x3 samples at
+// min + (max - min) * i * 0.5, eye-space bbox, and the largest summed sample
+// distance along x (vlen) and along y (hlen).  For Bezier patches the four
+// row splines in t = u are shared by the three samples with the same u; each
+// sample still performs exactly the reference's operations.
+struct RangeBound {
+    F3 bmin, bmax;
+    float vlen, hlen;
+};
+
+__device__ __forceinline__ RangeBound bound_range(const DrawDev& d, int pid, float4 r) {
+    F3 ps[3][3];
+    float sv[3], su[3];
+    for (int i = 0; i < 3; ++i) {
+        sv[i] = fadd(r.x, fmul(fmul(fsub(r.z, r.x), (float)i), 0.5f));
+        su[i] = fadd(r.y, fmul(fmul(fsub(r.w, r.y), (float)i), 0.5f));
+    }
+    if (d.type == 0) {
+        const float4* P = d.cp + (size_t)pid * 16;
+#pragma unroll
+        for (int iv = 0; iv < 3; ++iv) {
+            SplineW wt = spline_weights(su[iv]);
+            F3 row[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+                row[i] = spline3(wt, ld3(P + 4 * i + 0), ld3(P + 4 * i + 1), ld3(P + 4 * i + 2),
+                                 ld3(P + 4 * i + 3));
+#pragma unroll
+            for (int iu = 0; iu < 3; ++iu)
+                ps[iu][iv] = mv_point(d.mv, spline3(spline_weights(sv[iu]), row[0], row[1], row[2], row[3]));
+        }
+    } else {
+        const float4* P = d.cp + (size_t)pid * 20;
+#pragma unroll 1
+        for (int iu = 0; iu < 3; ++iu)
+#pragma unroll 1
+            for (int iv = 0; iv < 3; ++iv) ps[iu][iv] = mv_point(d.mv, eval_gregory_cpu(P, su[iv], sv[iu]));
+    }
+    RangeBound b;
+    const float inf = __int_as_float(0x7f800000);
+    b.bmin = F3{inf, inf, inf};
+    b.bmax = F3{-inf, -inf, -inf};
+#pragma unroll
+    for (int iu = 0; iu < 3; ++iu)
+#pragma unroll
+        for (int iv = 0; iv < 3; ++iv) {
+            const F3& p = ps[iu][iv];
+            b.bmin.x = minimum(p.x, b.bmin.x);
+            b.bmin.y = minimum(p.y, b.bmin.y);
+            b.bmin.z = minimum(p.z, b.bmin.z);
+            b.bmax.x = maximum(p.x, b.bmax.x);
+            b.bmax.y = maximum(p.y, b.bmax.y);
+            b.bmax.z = maximum(p.z, b.bmax.z);
+        }
+    b.vlen = 0.0f;
+    b.hlen = 0.0f;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        float h = 0.0f, v = 0.0f;
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+            v = fadd(v, distance3(ps[j][i], ps[j + 1][i]));
+            h = fadd(h, distance3(ps[i][j], ps[i][j + 1]));
+        }
+        b.vlen = maximum(v, b.vlen);
+        b.hlen = maximum(h, b.hlen);
+    }
+    return b;
+}
+
+// src/base/Projection.cpp:57-106.  Returns true when culled, else the screen size.
+__device__ __forceinline__ bool projection_cull(const DrawDev& d, const RangeBound& b, float& sx, float& sy) {
+    float n = -b.bmax.z;
+    float f = -b.bmin.z;
+    if (f < d.near_plane) return true;
+    n = maximum(d.near_plane, n);
+    float mnx = fadd(fmul(fdiv(b.bmin.x, b.bmin.x < 0 ? n : f), d.fx), d.vpx);
+    float mny = fadd(fmul(fdiv(b.bmin.y, b.bmin.y < 0 ? n : f), d.fy), d.vpy);
+    float mxx = fadd(fmul(fdiv(b.bmax.x, b.bmax.x > 0 ? n : f), d.fx), d.vpx);
+    float mxy = fadd(fmul(fdiv(b.bmax.y, b.bmax.y > 0 ? n : f), d.fy), d.vpy);
+    if (mnx > fadd((float)(d.vx - 1), d.cull_ribbon) || mxx < -d.cull_ribbon ||
+        mny > fadd((float)(d.vy - 1), d.cull_ribbon) || mxy < -d.cull_ribbon)
+        return true;
+    sx = fsub(mxx, mnx);
+    sy = fsub(mxy, mny);
+    return false;
+}
+
+enum BnsDecision { kCull = 0, kDraw = 1, kSplitY = 2, kSplitX = 3, kDrop = 4 };
+
+// src/Reyes/BoundNSplitCLCPU.cpp:117-148: cull, draw when in front of the eye
+// and smaller than the limit, drop past the depth cap, otherwise split the
+// direction with the longer sampled length (vlen < hlen halves y).
+__device__ __forceinline__ int bns_decide(const DrawDev& d, const FrameDev& fr, int pid, float4 r, int depth) {
+    RangeBound b = bound_range(d, pid, r);
+    float sx, sy;
+    if (projection_cull(d, b, sx, sy)) return kCull;
+    if (b.bmin.z < 0 && sx < fr.limit && sy < fr.limit) return kDraw;
+    if (depth > fr.max_depth) return kDrop;
+    return (b.vlen < b.hlen) ? kSplitY : kSplitX;
+}
+
+// Children of a split (BoundNSplitCLCPU.cpp:231-245): low half, high half.
+__device__ __forceinline__ void split_children(float4 r, int dec, float4& c0, float4& c1) {
+    if (dec == kSplitY) {
+        float cy = fmul(fadd(r.y, r.w), 0.5f);
+        c0 = make_float4(r.x, r.y, r.z, cy);
+        c1 = make_float4(r.x, cy, r.z, r.w);
+    } else {
+        float cx = fmul(fadd(r.x, r.z), 0.5f);
+        c0 = make_float4(r.x, r.y, cx, r.w);
+        c1 = make_float4(cx, r.y, r.z, r.w);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Kernel restatement arithmetic (R1-R6).
+
+__device__ __forceinline__ float ffma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+
+// R6: sin/cos by Cody-Waite reduction with pi/2 = P1 + P2 + P3 (three floats
+// from the exact value of pi) and Taylor polynomials (degree 9 / 10) on
+// |r| <= pi/4, evaluated with fused multiply-adds.
+__device__ __forceinline__ void sincos_reduced(float x, float& sr, float& cr, int& q) {
+    float k = rintf(fmul(x, 0x1.45f306p-1f));
+    float r = ffma(-k, 0x1.921fb6p+0f, x);
+    r = ffma(-k, -0x1.777a5cp-25f, r);
+    r = ffma(-k, -0x1.ee59dap-50f, r);
+    float kq = fsub(k, fmul(4.0f, floorf(fmul(k, 0.25f))));
+    q = (int)kq;
+    float r2 = fmul(r, r);
+    float ps = ffma(r2, 0x1.71de3ap-19f, -0x1.a01a02p-13f);
+    ps = ffma(r2, ps, 0x1.111112p-7f);
+    ps = ffma(r2, ps, -0x1.555556p-3f);
+    sr = ffma(fmul(r, r2), ps, r);
+    float pc = ffma(r2, -0x1.27e4fcp-22f, 0x1.a01a02p-16f);
+    pc = ffma(r2, pc, -0x1.6c16c2p-10f);
+    pc = ffma(r2, pc, 0x1.555556p-5f);
+    pc = ffma(r2, pc, -0x1.0p-1f);
+    cr = ffma(r2, pc, 1.0f);
+}
+__device__ __forceinline__ float mp_sinf(float x) {
+    if (!isfinite(x)) return fsub(x, x);
+    float s, c;
+    int q;
+    sincos_reduced(x, s, c, q);
+    q &= 3;
+    return q == 0 ? s : q == 1 ? c : q == 2 ? -s : -c;
+}
+__device__ __forceinline__ float mp_cosf(float x) {
+    if (!isfinite(x)) return fsub(x, x);
+    float s, c;
+    int q;
+    sincos_reduced(x, s, c, q);
+    q &= 3;
+    return q == 0 ? c : q == 1 ? -s : q == 2 ? -c : s;
+}
+
+__device__ __forceinline__ float sel_nan(float x) { return isnan(x) ? 0.0f : x; }
+
+// kernels/utility.h:121-152 -- p += (v_i * c_j) * P[4i + j], i-major; P.w = 1.
+__device__ __forceinline__ float4 eval_bezier_dice(const float4* P, float tx, float ty) {
+    float sx = fsub(1.0f, tx), sy = fsub(1.0f, ty);
+    float vw[4] = {fmul(fmul(sx, sx), sx), fmul(fmul(fmul(3.0f, sx), sx), tx), fmul(fmul(fmul(3.0f, sx), tx), tx),
+                   fmul(fmul(tx, tx), tx)};
+    float cw[4] = {fmul(fmul(sy, sy), sy), fmul(fmul(fmul(3.0f, ty), sy), sy), fmul(fmul(fmul(3.0f, ty), ty), sy),
+                   fmul(fmul(ty, ty), ty)};
+    float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            float w = fmul(vw[i], cw[j]);
+            float4 c = P[4 * i + j];
+            p.x = ffma(w, c.x, p.x);
+            p.y = ffma(w, c.y, p.y);
+            p.z = ffma(w, c.z, p.z);
+            p.w = ffma(w, c.w, p.w);
+        }
+    return p;
+}
+
+__device__ __forceinline__ float4 blend4(float a, float4 A, float b, float4 B, float den) {
+    return make_float4(sel_nan(fdiv(ffma(b, B.x, fmul(a, A.x)), den)), sel_nan(fdiv(ffma(b, B.y, fmul(a, A.y)), den)),
+                       sel_nan(fdiv(ffma(b, B.z, fmul(a, A.z)), den)), sel_nan(fdiv(ffma(b, B.w, fmul(a, A.w)), den)));
+}
+
+// kernels/utility.h:155-206 -- Gregory patch with NaN face blends zeroed.
+__device__ __forceinline__ float4 eval_gregory_dice(const float4* P, float tx, float ty) {
+    float sx = fsub(1.0f, tx), sy = fsub(1.0f, ty);
+    float u = tx, v = ty;
+    float4 F0 = blend4(u, P[12], v, P[16], fadd(u, v));
+    float4 F1 = blend4(fsub(1.0f, u), P[17], v, P[13], fadd(fsub(1.0f, u), v));
+    float4 F2 = blend4(fsub(1.0f, u), P[14], fsub(1.0f, v), P[18], fsub(fsub(2.0f, u), v));
+    float4 F3 = blend4(u, P[19], fsub(1.0f, v), P[15], fsub(fadd(1.0f, u), v));
+    float4 pts[16] = {P[0], P[4], P[9], P[1], P[8], F0, F1, P[5], P[7], F3, F2, P[10], P[3], P[11], P[6], P[2]};
+    float vw[4] = {fmul(fmul(sx, sx), sx), fmul(fmul(fmul(3.0f, sx), sx), tx), fmul(fmul(fmul(3.0f, sx), tx), tx),
+                   fmul(fmul(tx, tx), tx)};
+    float cw[4] = {fmul(fmul(sy, sy), sy), fmul(fmul(fmul(3.0f, ty), sy), sy), fmul(fmul(fmul(3.0f, ty), ty), sy),
+                   fmul(fmul(ty, ty), ty)};
+    float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            float w = fmul(vw[i], cw[j]);
+            float4 c = pts[4 * i + j];
+            p.x = ffma(w, c.x, p.x);
+            p.y = ffma(w, c.y, p.y);
+            p.z = ffma(w, c.z, p.z);
+            p.w = ffma(w, c.w, p.w);
+        }
+    return p;
+}
+
+// dot products: a chain of fused multiply-adds from x to w (R1)
+__device__ __forceinline__ float dot4r(const float* m, int r, float4 v) {
+    return ffma(m[12 + r], v.w, ffma(m[8 + r], v.z, ffma(m[4 + r], v.y, fmul(m[r], v.x))));
+}
+// kernels/utility.h:174-180
+__device__ __forceinline__ float4 mul_m44v4(const float* m, float4 v) {
+    return make_float4(dot4r(m, 0, v), dot4r(m, 1, v), dot4r(m, 2, v), dot4r(m, 3, v));
+}
+
+// kernels/dice.cl:51-67 -- eye-space displacement, updated coordinates used
+// immediately; fd are the three amplitudes.
+__device__ __forceinline__ float4 displace(float4 pos, const float* fd) {
+    const float k[3] = {5.0f, 7.0f, 11.0f};
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        pos.x = ffma(mp_sinf(fmul(fmul(pos.y, k[i]), 2.0f)), fd[i], pos.x);
+        pos.y = ffma(mp_sinf(fmul(fmul(pos.x, k[i]), 2.0f)), fd[i], pos.y);
+        pos.z = ffma(fmul(mp_sinf(fmul(fmul(pos.y, k[i]), 2.0f)), mp_sinf(fmul(fmul(pos.x, 3.0f), 2.0f))), fd[i],
+                     pos.z);
+    }
+    return pos;
+}
+
+// Eye-space position of dice vertex (nu, nv) of a sub-patch (kernels/dice.cl:44-67).
+__device__ __forceinline__ float4 dice_eye(const DrawDev& d, const FrameDev& fr, const float4* P, float4 r,
+                                           int nu, int nv) {
+    float tx = ffma(fsub(r.z, r.x), fdiv((float)nu, (float)fr.PS), r.x);
+    float ty = ffma(fsub(r.w, r.y), fdiv((float)nv, (float)fr.PS), r.y);
+    float4 o = (d.type == 0) ? eval_bezier_dice(P, tx, ty) : eval_gregory_dice(P, tx, ty);
+    float4 pos = mul_m44v4(d.mv, o);
+    if (fr.displacement) pos = displace(pos, fr.fdisp);
+    return pos;
+}
+
+// Projection to fixed-point pixel coordinates and NDC depth (kernels/dice.cl:69-79).
+__device__ __forceinline__ void project_vertex(const DrawDev& d, const FrameDev& fr, float4 pos, int& px, int& py,
+                                               float& depth) {
+    float4 p = mul_m44v4(d.proj, pos);
+    int vsx = fr.W << fr.shift, vsy = fr.H << fr.shift;
+    float ex = fadd(fmul(fmul(fdiv(p.x, p.w), (float)vsx), 0.5f), (float)(vsx / 2));
+    float ey = fadd(fmul(fmul(fdiv(p.y, p.w), (float)vsy), 0.5f), (float)(vsy / 2));
+    px = __float2int_rz(ex);
+    py = __float2int_rz(ey);
+    depth = fdiv(p.z, p.w);
+}
+
+struct V3 { float x, y, z; };
+__device__ __forceinline__ float dot3(V3 a, V3 b) { return ffma(a.z, b.z, ffma(a.y, b.y, fmul(a.x, b.x))); }
+__device__ __forceinline__ V3 cross3(V3 a, V3 b) {
+    return V3{ffma(-a.z, b.y, fmul(a.y, b.z)), ffma(-a.x, b.z, fmul(a.z, b.x)), ffma(-a.y, b.x, fmul(a.x, b.y))};
+}
+__device__ __forceinline__ V3 normalize3(V3 v) {
+    float l = __fsqrt_rn(dot3(v, v));
+    return V3{fdiv(v.x, l), fdiv(v.y, l), fdiv(v.z, l)};
+}
+
+// kernels/reyes.cl:172-191 -- flat colour of a quad from its 4 eye positions
+// (vertex order 0:(u,v) 1:(u+1,v) 2:(u,v+1) 3:(u+1,v+1)); the specular term
+// has colour 0 and contributes +0.
+__device__ __forceinline__ float4 shade_quad(const float4* pos, const float* dc) {
+    V3 du{fmul(fsub(fadd(fsub(pos[1].x, pos[0].x), pos[3].x), pos[2].x), 0.5f),
+          fmul(fsub(fadd(fsub(pos[1].y, pos[0].y), pos[3].y), pos[2].y), 0.5f),
+          fmul(fsub(fadd(fsub(pos[1].z, pos[0].z), pos[3].z), pos[2].z), 0.5f)};
+    V3 dv{fmul(fsub(fadd(fsub(pos[2].x, pos[0].x), pos[3].x), pos[1].x), 0.5f),
+          fmul(fsub(fadd(fsub(pos[2].y, pos[0].y), pos[3].y), pos[1].y), 0.5f),
+          fmul(fsub(fadd(fsub(pos[2].z, pos[0].z), pos[3].z), pos[1].z), 0.5f)};
+    V3 n = normalize3(cross3(dv, du));
+    V3 l = normalize3(V3{4.0f, 3.0f, 8.0f});
+    float m = fmaxf(dot3(n, l), 0.0f);
+    return make_float4(fadd(ffma(m, dc[0], fmul(0.015f, dc[0])), 0.0f), fadd(ffma(m, dc[1], fmul(0.015f, dc[1])), 0.0f),
+                       fadd(ffma(m, dc[2], fmul(0.015f, dc[2])), 0.0f), fadd(ffma(m, dc[3], fmul(1.0f, dc[3])), 0.0f));
+}
+
+// kernels/reyes.cl:240-265 edge setup of one triangle (wrapping int32, R5).
+struct Tri {
+    int Dx[3], Dy[3], O[3], C[3];
+    int Px[3], Py[3];
+    float dv[3];
+};
+__device__ __forceinline__ int wmul(int a, int b) { return (int)((unsigned)a * (unsigned)b); }
+__device__ __forceinline__ int wadd(int a, int b) { return (int)((unsigned)a + (unsigned)b); }
+__device__ __forceinline__ int wsub(int a, int b) { return (int)((unsigned)a - (unsigned)b); }
+
+__device__ __forceinline__ void tri_setup(Tri& t, int x0, int y0, float d0, int x1, int y1, float d1, int x2, int y2,
+                                          float d2) {
+    t.Px[0] = x0; t.Px[1] = x1; t.Px[2] = x2;
+    t.Py[0] = y0; t.Py[1] = y1; t.Py[2] = y2;
+    t.dv[0] = d0; t.dv[1] = d1; t.dv[2] = d2;
+#pragma unroll
+    for (int e = 0; e < 3; ++e) {
+        int en = (e + 1) % 3;
+        t.Dx[e] = wsub(t.Py[en], t.Py[e]);
+        t.Dy[e] = wsub(t.Px[e], t.Px[en]);
+    }
+#pragma unroll
+    for (int e = 0; e < 3; ++e) {
+        t.O[e] = wadd(wmul(t.Dx[e], t.Px[e]), wmul(t.Dy[e], t.Py[e]));
+        t.C[e] = (t.Dx[e] > 0 || (t.Dx[e] == 0 && t.Dy[e] > 0)) ? -1 : 0;
+    }
+}
+
+// inside_triangle(): updates depth when the sample is inside and nearer.
+__device__ __forceinline__ bool tri_test(const Tri& t, int tx, int ty, float& depth) {
+    int V[3];
+#pragma unroll
+    for (int e = 0; e < 3; ++e) V[e] = wsub(wadd(wmul(t.Dx[e], tx), wmul(t.Dy[e], ty)), t.O[e]);
+    bool ok = V[0] > t.C[0] && V[1] > t.C[1] && V[2] > t.C[2];
+    if (ok) {
+        float w[3];
+#pragma unroll
+        for (int e = 0; e < 3; ++e) {
+            int en = (e + 1) % 3;
+            int dn = wsub(wadd(wmul(t.Dx[en], t.Px[e]), wmul(t.Dy[en], t.Py[e])), t.O[en]);
+            w[e] = fdiv((float)V[en], (float)dn);
+        }
+        float d = ffma(t.dv[2], w[2], ffma(t.dv[1], w[1], fmul(t.dv[0], w[0])));
+        if (d < depth) depth = d;
+    }
+    return ok;
+}
+
+// idepth = (int)(clamp(depth / 200, 0, 1) * 0x7fffffff) (kernels/reyes.cl:364)
+__device__ __forceinline__ unsigned idepth_of(float depth) {
+    float c = fminf(fmaxf(fdiv(depth, 200.0f), 0.0f), 1.0f);
+    return (unsigned)__float2int_rz(fmul(c, 2147483648.0f));
+}
+
+// Tiled framebuffer index (kernels/reyes.cl:37-45, 8-pixel tiles).
+__device__ __forceinline__ long long fb_index(const FrameDev& fr, int x, int y) {
+    int tx = x >> 3, ty = y >> 3;
+    return ((long long)(tx + fr.gx * ty) << 6) + (x & 7) + ((y & 7) << 3);
+}
+
+}  // namespace mp

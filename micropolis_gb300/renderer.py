@@ -1,0 +1,216 @@
+"""Host-side mirror of the reference's renderer interface.
+
+`Renderer` has the reference's Reyes::Renderer methods (src/Reyes/Renderer.h:29-45):
+prepare(), are_patches_loaded(handle), load_patches(handle, patch_data, type),
+draw_patches(handle, modelview, projection, color), finish(), dump_trace(),
+with the same argument meaning.  Errors raise MpError (the reference throws
+CL::Exception).  Everything runs in libmpcore.so through the C ABI.
+"""
+from __future__ import annotations
+
+import ctypes
+from typing import Optional
+
+import numpy as np
+
+from . import _lib
+from ._lib import MpError, MpOptions, MpProjection, MpStats, lib
+from .options import ReyesOptions
+
+
+class Projection:
+    """Reyes::Projection(fovy, near, viewport) (src/base/Projection.h:144)."""
+
+    def __init__(self, fovy: float, near: float, viewport):
+        self.fovy = float(fovy)
+        self.near = float(near)
+        self.viewport = (int(viewport[0]), int(viewport[1]))
+
+    def c(self) -> MpProjection:
+        p = MpProjection()
+        p.fovy_deg = self.fovy
+        p.near_plane = self.near
+        p.viewport[0], p.viewport[1] = self.viewport
+        return p
+
+
+def _f32p(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+
+
+def _i32p(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+
+
+class Renderer:
+    def __init__(self, options: Optional[ReyesOptions] = None, **overrides):
+        opts = options or ReyesOptions()
+        if overrides:
+            opts = ReyesOptions(**{**opts.__dict__}).update(**overrides)
+        self.options = opts
+        o = MpOptions()
+        lib().mp_options_default(ctypes.byref(o))
+        o.window_size[0], o.window_size[1] = opts.window_size
+        o.reyes_patch_size = opts.reyes_patch_size
+        o.bound_n_split_limit = opts.bound_n_split_limit
+        o.reyes_patches_per_pass = opts.reyes_patches_per_pass
+        o.cull_ribbon = opts.cull_ribbon
+        o.max_split_depth = opts.max_split_depth
+        o.bound_sample_rate = opts.bound_sample_rate
+        o.subpixel_bits = opts.subpixel_bits
+        o.framebuffer_tile_size = opts.framebuffer_tile_size
+        o.backface_culling = int(bool(opts.backface_culling))
+        o.displacement = int(bool(opts.displacement))
+        o.displacement_amplitude = opts.displacement_amplitude
+        for i in range(4):
+            o.clear_color[i] = opts.clear_color[i]
+        o.batch_views = opts.batch_views
+        o.path = _lib.MP_PATH_PLAIN if opts.path == "plain" else _lib.MP_PATH_BATCHED
+        self._ctx = ctypes.c_void_p()
+        st = lib().mp_create(ctypes.byref(o), ctypes.byref(self._ctx))
+        if st != 0:
+            raise MpError(st, "mp_create failed")
+        self.width, self.height = opts.window_size
+        self.views = opts.batch_views
+
+    # -- error plumbing --------------------------------------------------------
+    def _ck(self, st: int) -> None:
+        if st != 0:
+            raise MpError(st, lib().mp_last_error(self._ctx).decode())
+
+    def close(self) -> None:
+        if self._ctx:
+            lib().mp_destroy(self._ctx)
+            self._ctx = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_stream(self, stream_handle: int) -> None:
+        self._ck(lib().mp_set_stream(self._ctx, ctypes.c_void_p(stream_handle or None)))
+
+    # -- Reyes::Renderer --------------------------------------------------------
+    def prepare(self) -> None:
+        self._ck(lib().mp_prepare(self._ctx))
+
+    def finish(self) -> None:
+        self._ck(lib().mp_finish(self._ctx))
+
+    def are_patches_loaded(self, handle: int) -> bool:
+        v = ctypes.c_int32()
+        self._ck(lib().mp_are_patches_loaded(self._ctx, handle, ctypes.byref(v)))
+        return bool(v.value)
+
+    def load_patches(self, handle: int, patch_data, patch_type: int) -> None:
+        a = np.ascontiguousarray(patch_data, np.float32).reshape(-1, 3)
+        self._ck(lib().mp_load_patches(self._ctx, handle, _f32p(a), a.shape[0], patch_type))
+
+    def load_patches_device(self, handle: int, dev_ptr: int, n_points: int, patch_type: int) -> None:
+        self._ck(lib().mp_load_patches_device(self._ctx, handle, ctypes.c_void_p(dev_ptr), n_points, patch_type))
+
+    def update_patches_device(self, handle: int, dev_ptr: int) -> None:
+        self._ck(lib().mp_update_patches_device(self._ctx, handle, ctypes.c_void_p(dev_ptr)))
+
+    def delete_patches(self, handle: int) -> None:
+        self._ck(lib().mp_delete_patches(self._ctx, handle))
+
+    def draw_patches(self, handle: int, modelview, projection: Projection, color=(1, 1, 1, 1), view: int = 0) -> None:
+        mv = np.ascontiguousarray(modelview, np.float32).reshape(16)
+        col = np.ascontiguousarray(color, np.float32).reshape(4)
+        p = projection.c()
+        self._ck(lib().mp_draw_patches_view(self._ctx, handle, _f32p(mv), ctypes.byref(p), _f32p(col), view))
+
+    def dump_trace(self) -> str:
+        buf = ctypes.create_string_buffer(4096)
+        self._ck(lib().mp_dump_trace(self._ctx, buf, len(buf)))
+        return buf.value.decode()
+
+    # -- headless framebuffer and inspection -------------------------------------
+    def framebuffer_ptrs(self):
+        c, d = ctypes.c_void_p(), ctypes.c_void_p()
+        self._ck(lib().mp_framebuffer(self._ctx, ctypes.byref(c), ctypes.byref(d), None, None, None))
+        return c.value, d.value
+
+    def read_framebuffer(self, view: int = 0, linear: bool = False):
+        n = self.width * self.height
+        color = np.zeros((n, 4), np.float32)
+        depth = np.zeros(n, np.int32)
+        self._ck(lib().mp_read_framebuffer(self._ctx, view, _f32p(color), _i32p(depth), int(linear)))
+        return color, depth
+
+    def subpatches(self):
+        cnt = ctypes.c_int64()
+        self._ck(lib().mp_subpatches(self._ctx, ctypes.byref(cnt), None, None, None, 0))
+        n = cnt.value
+        draw = np.zeros(max(n, 1), np.int32)
+        pid = np.zeros(max(n, 1), np.int32)
+        rng = np.zeros((max(n, 1), 4), np.float32)
+        self._ck(lib().mp_subpatches(self._ctx, ctypes.byref(cnt), _i32p(draw), _i32p(pid), _f32p(rng), n))
+        return draw[:n], pid[:n], rng[:n]
+
+    STAGES = ("clear", "bound_split", "dice_raster", "raster_big", "resolve_or_shade", "sample", "pass_resolve",
+              "host_sync")
+
+    def stats(self) -> dict:
+        s = MpStats()
+        self._ck(lib().mp_stats_get(self._ctx, ctypes.byref(s)))
+        out = {k: getattr(s, k) for k, _ in MpStats._fields_ if k != "stage_ms"}
+        out["stage_ms"] = dict(zip(self.STAGES, list(s.stage_ms)))
+        return out
+
+    def set_stage_timing(self, on: bool) -> None:
+        self._ck(lib().mp_set_stage_timing(self._ctx, int(bool(on))))
+
+    def dice_subpatches(self, draw: int, pid, rng):
+        pid = np.ascontiguousarray(pid, np.int32)
+        rng = np.ascontiguousarray(rng, np.float32).reshape(-1, 4)
+        n = len(pid)
+        G = self.options.reyes_patch_size + 1
+        pos = np.zeros((n, G * G, 4), np.float32)
+        pxl = np.zeros((n, G * G, 2), np.int32)
+        dep = np.zeros((n, G * G), np.float32)
+        self._ck(lib().mp_dice_subpatches(self._ctx, draw, n, _i32p(pid), _f32p(rng), _f32p(pos), _i32p(pxl),
+                                          _f32p(dep)))
+        return pos, pxl, dep
+
+    def set_grad_buffer(self, draw: int, dev_ptr: int) -> None:
+        self._ck(lib().mp_set_grad_buffer(self._ctx, draw, ctypes.c_void_p(dev_ptr)))
+
+    def backward(self, view: int, grad_color_ptr: int, grad_amp_ptr: int) -> None:
+        self._ck(lib().mp_backward(self._ctx, view, ctypes.c_void_p(grad_color_ptr), ctypes.c_void_p(grad_amp_ptr)))
+
+    def inclusive_scan(self, values) -> np.ndarray:
+        a = np.ascontiguousarray(values, np.int32)
+        out = np.zeros_like(a)
+        self._ck(lib().mp_inclusive_scan(self._ctx, _i32p(a), _i32p(out), len(a)))
+        return out
+
+    def atomic_bench(self, n_slots: int, n_ops: int, pattern: int) -> float:
+        r = ctypes.c_double()
+        self._ck(lib().mp_atomic_bench(self._ctx, n_slots, n_ops, pattern, ctypes.byref(r)))
+        return r.value
+
+
+def render_scene(renderer: Renderer, scene, handles=None) -> None:
+    """Scene::draw (src/micropolis/Scene.cpp:179-197): prepare, load on first
+    use, draw every object, finish."""
+    renderer.prepare()
+    for k, d in enumerate(scene.draws):
+        h = handles[k] if handles else id(d.mesh)
+        if not renderer.are_patches_loaded(h):
+            renderer.load_patches(h, d.mesh.cp, d.mesh.type)
+        renderer.draw_patches(h, d.mv, Projection(scene.fovy, scene.near, (scene.width, scene.height)), d.color,
+                              view=d.view)
+    renderer.finish()
+
+
+def renderer_for(scene, path: str = "batched", **over) -> Renderer:
+    opts = ReyesOptions(window_size=(scene.width, scene.height), path=path)
+    known = {k: v for k, v in scene.options.items() if hasattr(opts, k)}
+    opts.update(**known)
+    if over:
+        opts.update(**over)
+    return Renderer(opts)

@@ -1,0 +1,265 @@
+"""ctypes binding of the CPU oracle: TEST INFRASTRUCTURE ONLY.
+
+Imported by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg,
+as the checker or the timed CPU baseline; never by the product package.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liboracle.so")
+REF_PIN_PATH = os.path.join(HERE, "_ref", "libref_pin.so")
+
+f32p = ctypes.POINTER(ctypes.c_float)
+i32p = ctypes.POINTER(ctypes.c_int32)
+i64p = ctypes.POINTER(ctypes.c_int64)
+f64p = ctypes.POINTER(ctypes.c_double)
+
+
+class OrDraw(ctypes.Structure):
+    _fields_ = [("cp", f32p), ("n_patches", ctypes.c_int32), ("type", ctypes.c_int32),
+                ("mv", ctypes.c_float * 16), ("color", ctypes.c_float * 4)]
+
+
+class OrParams(ctypes.Structure):
+    _fields_ = [("width", ctypes.c_int32), ("height", ctypes.c_int32),
+                ("fovy_deg", ctypes.c_float), ("near_plane", ctypes.c_float),
+                ("bound_n_split_limit", ctypes.c_float), ("cull_ribbon", ctypes.c_float),
+                ("max_split_depth", ctypes.c_int32), ("reyes_patches_per_pass", ctypes.c_int32),
+                ("reyes_patch_size", ctypes.c_int32), ("subpixel_bits", ctypes.c_int32),
+                ("backface_culling", ctypes.c_int32), ("displacement", ctypes.c_int32),
+                ("displacement_amplitude", ctypes.c_float), ("clear_color", ctypes.c_float * 4)]
+
+
+def build() -> None:
+    subprocess.check_call(["sh", os.path.join(HERE, "build.sh")], stdout=subprocess.DEVNULL)
+
+
+def build_ref() -> None:
+    subprocess.check_call(["sh", os.path.join(HERE, "build_ref.sh")], stdout=subprocess.DEVNULL)
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        L = ctypes.CDLL(LIB_PATH)
+        L.or_bound_n_split.restype = ctypes.c_int64
+        L.or_bound_n_split.argtypes = [ctypes.POINTER(OrParams), ctypes.POINTER(OrDraw), i32p, f32p,
+                                       ctypes.c_int64, i64p]
+        L.or_render.restype = ctypes.c_int
+        L.or_render.argtypes = [ctypes.POINTER(OrParams), ctypes.POINTER(OrDraw), ctypes.c_int32, f32p,
+                                i32p, i64p]
+        L.or_render_subpatches.restype = ctypes.c_int
+        L.or_render_subpatches.argtypes = [ctypes.POINTER(OrParams), ctypes.POINTER(OrDraw), ctypes.c_int32,
+                                           ctypes.c_int64, i32p, i32p, f32p, f32p, i32p, i64p, i64p]
+        L.or_dice.restype = None
+        L.or_dice.argtypes = [ctypes.POINTER(OrParams), ctypes.POINTER(OrDraw), ctypes.c_int32, f32p, f32p,
+                              i32p, f32p]
+        L.or_dice_fp64.restype = None
+        L.or_dice_fp64.argtypes = [ctypes.POINTER(OrParams), ctypes.POINTER(OrDraw), ctypes.c_int32, f32p,
+                                   f64p]
+        L.or_loss_fp64.restype = ctypes.c_double
+        L.or_loss_fp64.argtypes = [ctypes.POINTER(OrParams), ctypes.POINTER(OrDraw), ctypes.c_int64, i32p,
+                                   f32p, i64p, f32p, f64p, ctypes.c_double, f64p, f64p]
+        L.or_sinf.restype = ctypes.c_float
+        L.or_sinf.argtypes = [ctypes.c_float]
+        L.or_cosf.restype = ctypes.c_float
+        L.or_cosf.argtypes = [ctypes.c_float]
+        L.or_inclusive_scan.restype = None
+        L.or_inclusive_scan.argtypes = [i32p, i32p, ctypes.c_int64]
+        _lib = L
+    return _lib
+
+
+def _ptr(a, t):
+    return a.ctypes.data_as(t)
+
+
+def make_params(scene, **over) -> OrParams:
+    o = dict(bound_n_split_limit=8.0, cull_ribbon=32.0, max_split_depth=23, reyes_patches_per_pass=100000,
+             reyes_patch_size=8, subpixel_bits=6, backface_culling=1, displacement=0,
+             displacement_amplitude=1.0, clear_color=(0.1, 0.1, 0.7, 0.0))
+    o.update({k: v for k, v in scene.options.items() if k in o})
+    o.update(over)
+    p = OrParams()
+    p.width, p.height = scene.width, scene.height
+    p.fovy_deg, p.near_plane = scene.fovy, scene.near
+    for k in ("bound_n_split_limit", "cull_ribbon", "displacement_amplitude"):
+        setattr(p, k, float(o[k]))
+    for k in ("max_split_depth", "reyes_patches_per_pass", "reyes_patch_size", "subpixel_bits",
+              "backface_culling", "displacement"):
+        setattr(p, k, int(o[k]))
+    for i in range(4):
+        p.clear_color[i] = o["clear_color"][i]
+    return p
+
+
+class _Draws:
+    """Keeps the numpy buffers alive while the oracle reads them."""
+
+    def __init__(self, draws):
+        self.keep = []
+        self.arr = (OrDraw * max(1, len(draws)))()
+        for k, d in enumerate(draws):
+            cp = np.ascontiguousarray(d.mesh.cp, np.float32).reshape(-1)
+            self.keep.append(cp)
+            self.arr[k].cp = _ptr(cp, f32p)
+            self.arr[k].n_patches = d.mesh.n_patches
+            self.arr[k].type = d.mesh.type
+            for i in range(16):
+                self.arr[k].mv[i] = float(d.mv[i])
+            for i in range(4):
+                self.arr[k].color[i] = float(d.color[i])
+        self.n = len(draws)
+
+
+def bound_n_split(scene, draw_index=0, params=None, cap=None):
+    """Reference-order sub-patches of one draw: (pid int32[S], range float32[S,4], n_bounds)."""
+    p = params or make_params(scene)
+    ds = _Draws([scene.draws[draw_index]])
+    n_b = ctypes.c_int64(0)
+    n = lib().or_bound_n_split(ctypes.byref(p), ds.arr, None, None, 0, ctypes.byref(n_b))
+    cap = n if cap is None else cap
+    pid = np.zeros(max(cap, 1), np.int32)
+    rng = np.zeros((max(cap, 1), 4), np.float32)
+    lib().or_bound_n_split(ctypes.byref(p), ds.arr, _ptr(pid, i32p), _ptr(rng, f32p), cap, ctypes.byref(n_b))
+    return pid[:n], rng[:n], int(n_b.value)
+
+
+def render(scene, params=None, draws=None):
+    """Full frame: (tiled colour float32[W*H,4], tiled depth int32[W*H], stats dict)."""
+    p = params or make_params(scene)
+    draws = scene.draws if draws is None else draws
+    ds = _Draws(draws)
+    npx = scene.width * scene.height
+    color = np.zeros((npx, 4), np.float32)
+    depth = np.zeros(npx, np.int32)
+    st = np.zeros(4, np.int64)
+    rc = lib().or_render(ctypes.byref(p), ds.arr, ds.n, _ptr(color, f32p), _ptr(depth, i32p), _ptr(st, i64p))
+    if rc:
+        raise ValueError(f"oracle render failed: {rc}")
+    return color, depth, dict(subpatches=int(st[0]), micropolygons=int(st[1]), fragments=int(st[2]),
+                              bounds=int(st[3]))
+
+
+def render_subpatches(scene, sub_draw, sub_pid, sub_range, params=None, want_win=False):
+    p = params or make_params(scene)
+    ds = _Draws(scene.draws)
+    npx = scene.width * scene.height
+    color = np.zeros((npx, 4), np.float32)
+    depth = np.zeros(npx, np.int32)
+    win = np.zeros(npx, np.int64) if want_win else None
+    st = np.zeros(4, np.int64)
+    sd = np.ascontiguousarray(sub_draw, np.int32)
+    sp = np.ascontiguousarray(sub_pid, np.int32)
+    sr = np.ascontiguousarray(sub_range, np.float32).reshape(-1)
+    rc = lib().or_render_subpatches(ctypes.byref(p), ds.arr, ds.n, len(sp), _ptr(sd, i32p), _ptr(sp, i32p),
+                                    _ptr(sr, f32p), _ptr(color, f32p), _ptr(depth, i32p),
+                                    _ptr(win, i64p) if want_win else None, _ptr(st, i64p))
+    if rc:
+        raise ValueError(f"oracle render failed: {rc}")
+    stats = dict(subpatches=int(st[0]), micropolygons=int(st[1]), fragments=int(st[2]))
+    return (color, depth, win, stats) if want_win else (color, depth, stats)
+
+
+def dice(scene, draw_index, pid, rng, params=None):
+    p = params or make_params(scene)
+    ds = _Draws([scene.draws[draw_index]])
+    G = p.reyes_patch_size + 1
+    pos = np.zeros((G * G, 4), np.float32)
+    pxl = np.zeros((G * G, 2), np.int32)
+    dep = np.zeros(G * G, np.float32)
+    r = np.ascontiguousarray(rng, np.float32)
+    lib().or_dice(ctypes.byref(p), ds.arr, int(pid), _ptr(r, f32p), _ptr(pos, f32p), _ptr(pxl, i32p),
+                  _ptr(dep, f32p))
+    return pos, pxl, dep
+
+
+def dice_fp64(scene, draw_index, pid, rng, params=None):
+    p = params or make_params(scene)
+    ds = _Draws([scene.draws[draw_index]])
+    G = p.reyes_patch_size + 1
+    out = np.zeros((G * G, 3), np.float64)
+    r = np.ascontiguousarray(rng, np.float32)
+    lib().or_dice_fp64(ctypes.byref(p), ds.arr, int(pid), _ptr(r, f32p), _ptr(out, f64p))
+    return out
+
+
+def loss_fp64(scene, sub_pid, sub_range, win, target, cp, amp, params=None, grad=True):
+    """FP64 loss with fixed visibility and its analytic gradient (draw 0)."""
+    p = params or make_params(scene)
+    ds = _Draws([scene.draws[0]])
+    sp = np.ascontiguousarray(sub_pid, np.int32)
+    sr = np.ascontiguousarray(sub_range, np.float32).reshape(-1)
+    w = np.ascontiguousarray(win, np.int64)
+    t = np.ascontiguousarray(target, np.float32).reshape(-1)
+    c = np.ascontiguousarray(cp, np.float64).reshape(-1)
+    g = np.zeros_like(c) if grad else None
+    ga = ctypes.c_double(0)
+    loss = lib().or_loss_fp64(ctypes.byref(p), ds.arr, len(sp), _ptr(sp, i32p), _ptr(sr, f32p), _ptr(w, i64p),
+                              _ptr(t, f32p), _ptr(c, f64p), float(amp), _ptr(g, f64p) if grad else None,
+                              ctypes.byref(ga) if grad else None)
+    return (loss, g.reshape(np.shape(cp)), ga.value) if grad else loss
+
+
+def sinf(x: float) -> float:
+    return lib().or_sinf(x)
+
+
+def inclusive_scan(a):
+    a = np.ascontiguousarray(a, np.int32)
+    out = np.zeros_like(a)
+    lib().or_inclusive_scan(_ptr(a, i32p), _ptr(out, i32p), len(a))
+    return out
+
+
+# --- reference pin (only where the reference tree was compiled) -------------
+
+_ref = None
+
+
+def ref_pin():
+    """The reference's own src/base math, compiled by build_ref.sh, or None."""
+    global _ref
+    if _ref is None:
+        if not os.path.exists(REF_PIN_PATH):
+            return None
+        L = ctypes.CDLL(REF_PIN_PATH)
+        L.refpin_eval_patch.argtypes = [f32p, ctypes.c_float, ctypes.c_float, f32p]
+        L.refpin_eval_gregory.argtypes = [f32p, ctypes.c_float, ctypes.c_float, f32p]
+        L.refpin_projection_bound.restype = ctypes.c_int
+        L.refpin_projection_bound.argtypes = [ctypes.c_float, ctypes.c_float, ctypes.c_int, ctypes.c_int,
+                                              ctypes.c_float, f32p, f32p]
+        L.refpin_bound_n_split.restype = ctypes.c_long
+        L.refpin_bound_n_split.argtypes = [f32p, ctypes.c_int, ctypes.c_int, f32p, ctypes.c_float, ctypes.c_float,
+                                           ctypes.c_int, ctypes.c_int, ctypes.c_float, ctypes.c_float,
+                                           ctypes.c_int, i32p, f32p, ctypes.c_long]
+        _ref = L
+    return _ref
+
+
+def ref_bound_n_split(scene, draw_index=0, params=None):
+    L = ref_pin()
+    if L is None:
+        return None
+    p = params or make_params(scene)
+    d = scene.draws[draw_index]
+    cp = np.ascontiguousarray(d.mesh.cp, np.float32).reshape(-1)
+    mv = np.ascontiguousarray(d.mv, np.float32)
+    args = (_ptr(cp, f32p), d.mesh.n_patches, d.mesh.type, _ptr(mv, f32p), p.fovy_deg, p.near_plane, p.width,
+            p.height, p.cull_ribbon, p.bound_n_split_limit, p.max_split_depth)
+    n = L.refpin_bound_n_split(*args, None, None, 0)
+    pid = np.zeros(max(n, 1), np.int32)
+    rng = np.zeros((max(n, 1), 4), np.float32)
+    L.refpin_bound_n_split(*args, _ptr(pid, i32p), _ptr(rng, f32p), n)
+    return pid[:n], rng[:n]
