@@ -1,0 +1,389 @@
+#!/usr/bin/env python3
+"""Benchmark of the REYES core on one GB300 (replicas on N GPUs).
+
+Workload (one step = one frame): mixed4096_1920x1080 -- 4096 patches (2048
+bicubic Bezier + 2048 Gregory), centres U[-10,10]^3, lognormal sides, random
+orientation, 1920x1080, bound_n_split_limit 8 px, reyes_patch_size 8, rendered
+by the batched path (one persistent launch per stage, CUDA-graph replay).
+
+Metric: micropolygons/s = reyes_patch_size^2 x emitted sub-patches per frame
+(src/base/Statistics.cpp:175) / frame time.  `value` is device time (CUDA
+events on the renderer's stream around each frame, L2 flushed between
+frames outside the events); `e2e` is the same metric through the C ABI with
+the control points uploaded from pinned host memory and the framebuffer
+(colour + depth) read back to pinned host memory inside the timed step.
+
+--impl reference times the reference's CPU path: its CPU bound-and-split and
+its dice/shade/sample kernels as restated by the oracle (no OpenCL runtime
+exists on this machine), on all host cores, over a bounded sample.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = "mixed4096_1920x1080"
+METRIC = "micropolygons/s (batched path, 4096-patch mixed Bezier/Gregory scene, 1920x1080)"
+L2_FLUSH_BYTES = 256 << 20
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-extras", action="store_true", help="skip plain/adjoint/cpu legs")
+    return ap.parse_args()
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    def __init__(self, index: int):
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out" if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else ".",
+                                 f".clocks_{os.getpid()}.csv")
+        self.index = index
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}",
+                 "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+                 "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_power_cap", "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            self.proc.wait()
+
+    def summary(self):
+        if not self.proc or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 7:
+                rows.append(parts)
+        os.remove(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[0]) for r in rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[3 + i].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+# --------------------------------------------------------------------------
+# CPU baseline (the oracle's restatement of the reference CPU path)
+
+def _cpu_chunk(args):
+    """Render a bounded sample (patch subset) of the workload on one core."""
+    name, draw_slices = args
+    sys.path.insert(0, ROOT)
+    from micropolis_gb300 import scenes
+    from oracle import oracle
+    sc = scenes.WORKLOADS[name]()
+    for d, (a, b) in zip(sc.draws, draw_slices):
+        d.mesh = scenes.Mesh(d.mesh.type, d.mesh.cp[a:b])
+    t = time.perf_counter()
+    _, _, st = oracle.render(sc)
+    return st["micropolygons"], time.perf_counter() - t
+
+
+def cpu_baseline(name: str, procs: int, patches_per_proc: int):
+    """micropolygons/s of the oracle path on `procs` processes, each rendering
+    its own disjoint slice of every draw's patches (a bounded sample)."""
+    import multiprocessing as mp
+    from micropolis_gb300 import scenes
+    from oracle import oracle
+    oracle.lib()
+    sc = scenes.WORKLOADS[name]()
+    jobs = []
+    for p in range(procs):
+        sl = []
+        for d in sc.draws:
+            share = max(1, patches_per_proc // len(sc.draws))
+            a = (p * share) % max(1, d.mesh.n_patches)
+            sl.append((a, min(a + share, d.mesh.n_patches)))
+        jobs.append((name, sl))
+    t = time.perf_counter()
+    if procs == 1:
+        res = [_cpu_chunk(jobs[0])]
+    else:
+        with mp.get_context("spawn").Pool(procs) as pool:
+            res = pool.map(_cpu_chunk, jobs)
+    wall = time.perf_counter() - t
+    mpoly = sum(r[0] for r in res)
+    busy = max(r[1] for r in res)
+    return mpoly / busy, mpoly, wall, busy
+
+
+# --------------------------------------------------------------------------
+
+def run_reference(args):
+    rank, world, _ = dist_info()
+    if rank != 0:
+        return 0
+    cores = os.cpu_count() or 1
+    per = 96
+    vals = []
+    for i in range(args.warmup + args.steps):
+        v, mpoly, wall, busy = cpu_baseline(WORKLOAD, cores, per)
+        if i >= args.warmup:
+            vals.append((v, mpoly, busy))
+    value = sum(v[1] for v in vals) / sum(v[2] for v in vals)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "micropolygons/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(v[2] for v in vals),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded generator, no dataset)",
+            "config": {"workload": WORKLOAD, "sample": f"{cores} processes x {per} patches per step"},
+            "cpu_baseline": {"value": value, "unit": "micropolygons/s", "cores": cores, "kind": "port",
+                             "sample": f"{cores} processes, each bound&split+dice+shade+sample of {per} of the "
+                                       f"4096 patches per step; CPU bound&split single-threaded per process"},
+            "e2e": {"value": value, "unit": "micropolygons/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    import numpy as np
+    import torch
+
+    rank, world, local = dist_info()
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+
+    from micropolis_gb300 import build as mpbuild
+    mpbuild.build()
+    from micropolis_gb300 import scenes
+    from micropolis_gb300.renderer import Projection, renderer_for
+
+    sc = scenes.WORKLOADS[WORKLOAD]()
+    stream = torch.cuda.Stream(dev)
+    r = renderer_for(sc, "batched")
+    r.set_stream(stream.cuda_stream)
+    proj = Projection(sc.fovy, sc.near, (sc.width, sc.height))
+    handles = [1000 + k for k in range(len(sc.draws))]
+    for h, d in zip(handles, sc.draws):
+        r.load_patches(h, d.mesh.cp, d.mesh.type)
+
+    def frame():
+        r.prepare()
+        for h, d in zip(handles, sc.draws):
+            r.draw_patches(h, d.mv, proj, d.color)
+        r.finish()
+
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    for _ in range(args.warmup):
+        frame()
+    st0 = r.stats()
+    mpoly = st0["micropolygons"]
+
+    # ---- timed region: K frames, device time per frame
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    graph_ms = []
+    with ClockSampler(local) as clk:
+        t_wall = time.perf_counter()
+        for k in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(float(k))           # L2 flush, outside the frame's events
+            evs[k][0].record(stream)
+            frame()
+            evs[k][1].record(stream)
+            graph_ms.append(r.stats()["gpu_ms"])
+        torch.cuda.synchronize()
+        t_wall = time.perf_counter() - t_wall
+    frame_ms = [a.elapsed_time(b) for a, b in evs]
+    t_dev = sum(frame_ms) / 1e3
+    if world > 1:
+        t = torch.tensor([t_dev], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        t_dev = float(t.item())
+        torch.distributed.barrier()
+    total_mp = mpoly * args.steps * world
+    value = total_mp / t_dev
+    stats = r.stats()
+    _, depth_now = r.read_framebuffer()
+    covered = int(np.count_nonzero(depth_now != 0x7FFFFFFF))
+
+    # ---- e2e: host buffers through the C ABI (pinned), copies inside each step
+    W, H = sc.width, sc.height
+    host_cp = [torch.from_numpy(np.ascontiguousarray(d.mesh.cp, np.float32)).pin_memory().numpy()
+               for d in sc.draws]
+    col_host = torch.empty((W * H, 4), dtype=torch.float32).pin_memory().numpy()
+    dep_host = torch.empty((W * H,), dtype=torch.int32).pin_memory().numpy()
+    h2d = sum(int(c.shape[0] * c.shape[1]) * 16 for c in host_cp)
+    d2h = W * H * 16 + W * H * 4
+
+    def e2e_step():
+        for h, c, d in zip(handles, host_cp, sc.draws):
+            r.load_patches(h, c, d.mesh.type)
+        r.prepare()
+        for h, d in zip(handles, sc.draws):
+            r.draw_patches(h, d.mv, proj, d.color)
+        r.finish()
+        from micropolis_gb300 import _lib
+        import ctypes
+        _lib.lib().mp_read_framebuffer(r._ctx, 0, col_host.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+                                       dep_host.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), 0)
+
+    for _ in range(2):
+        e2e_step()
+    torch.cuda.synchronize()
+    e2e_times = []
+    for _ in range(args.steps):
+        t = time.perf_counter()
+        e2e_step()
+        e2e_times.append(time.perf_counter() - t)
+    e2e_value = mpoly / statistics.mean(e2e_times) * world
+
+    # ---- stage timing pass (same frame, stages as separate launches)
+    r.set_stage_timing(True)
+    stage = {k: [] for k in r.STAGES}
+    for _ in range(5):
+        with torch.cuda.stream(stream):
+            flush.fill_(1.0)
+        frame()
+        for k, v in r.stats()["stage_ms"].items():
+            stage[k].append(v)
+    r.set_stage_timing(False)
+    stage_ms = {k: statistics.median(v) for k, v in stage.items() if max(v) > 0}
+    dominant = max(stage_ms, key=stage_ms.get)
+
+    peak_gbs, peak_kind = measured_peaks()
+    n_cp_bytes = sum(d.mesh.n_patches * d.mesh.cp.shape[1] * 16 for d in sc.draws)
+    S = stats["subpatches"]
+    frags = stats["fragments"]
+    # algorithmic bytes of the dice+raster kernel: sub-patch records (24 B),
+    # control points once (16 B per point), one 8-byte atomic per fragment
+    alg = {"dice_raster": S * 24 + n_cp_bytes + frags * 8,
+           "bound_split": stats["bounds"] * 24 * 2 + n_cp_bytes + S * 24,
+           "resolve_or_shade": W * H * (8 + 16 + 4) + S * 0,
+           "clear": W * H * 8}
+    dom_bytes = alg.get(dominant, 0)
+    dom_s = stage_ms[dominant] / 1e3
+    achieved = dom_bytes / dom_s / 1e9 if dom_s > 0 else 0.0
+    roofline = {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak_gbs, "unit": "GB/s",
+                "frac": achieved / peak_gbs, "traffic": None, "peak_kind": peak_kind,
+                "stage_ms": stage_ms, "alg_bytes": dom_bytes}
+
+    extras = {}
+    if not args.no_extras and rank == 0:
+        # plain per-pass path on the same frame
+        rp = renderer_for(sc, "plain")
+        rp.set_stream(stream.cuda_stream)
+        for h, d in zip(handles, sc.draws):
+            rp.load_patches(h, d.mesh.cp, d.mesh.type)
+
+        def pframe():
+            rp.prepare()
+            for h, d in zip(handles, sc.draws):
+                rp.draw_patches(h, d.mv, proj, d.color)
+            rp.finish()
+
+        for _ in range(2):
+            pframe()
+        pms = []
+        for _ in range(max(3, args.steps // 4)):
+            with torch.cuda.stream(stream):
+                flush.fill_(2.0)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            pframe()
+            b.record(stream)
+            torch.cuda.synchronize()
+            pms.append(a.elapsed_time(b))
+        pst = rp.stats()
+        plain_ms = statistics.mean(pms)
+        extras["plain"] = {"ms_per_frame": plain_ms, "value": pst["micropolygons"] / (plain_ms / 1e3),
+                           "passes": pst["passes"], "micropolygons": pst["micropolygons"]}
+        extras["batched_over_plain"] = value / extras["plain"]["value"]
+        rp.close()
+        # backward / forward on the displaced 16x16 heightfield at 512x512
+        try:
+            from micropolis_gb300 import adjoint
+            extras["adjoint"] = adjoint.bench_bwd_fwd(stream)
+        except Exception as e:  # noqa: BLE001
+            extras["adjoint"] = {"error": str(e)[:200]}
+        # CPU baseline: bounded sample on the host cores
+        cores = os.cpu_count() or 1
+        per = 96
+        cv, cmp, cwall, cbusy = cpu_baseline(WORKLOAD, cores, per)
+        extras["cpu_baseline"] = {"value": cv, "unit": "micropolygons/s", "cores": cores, "kind": "port",
+                                  "sample": f"{cores} processes, each bound&split+dice+shade+sample of {per} of "
+                                            f"the 4096 patches ({cmp} micropolygons in {cbusy:.1f} s)"}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "micropolygons/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_dev / args.steps,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic (seeded generator, no dataset)",
+                "config": {"workload": WORKLOAD, "patches": sc.n_patches, "width": W, "height": H,
+                           "bound_n_split_limit": 8, "reyes_patch_size": 8, "path": "batched (CUDA graph)",
+                           "parallelism": f"replicas x{world}", "l2": "flushed (256 MiB write) between frames",
+                           "micropolygons_per_frame": mpoly, "subpatches": S, "fragments": frags,
+                           "fragments_per_pixel": frags / (W * H),
+                           "depth_complexity_covered": frags / max(covered, 1), "bounds": stats["bounds"],
+                           "graph_ms_median": statistics.median(graph_ms),
+                           "wall_ms_per_frame": 1e3 * t_wall / args.steps},
+                "e2e": {"value": e2e_value, "unit": "micropolygons/s", "h2d_bytes_per_step": h2d,
+                        "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * statistics.mean(e2e_times)},
+                "gpu_launches": 6 * args.steps,
+                "roofline": roofline,
+                "clocks": clk.summary()}
+        if "cpu_baseline" in extras:
+            line["cpu_baseline"] = extras.pop("cpu_baseline")
+        line.update(extras)
+        print(json.dumps(line))
+    r.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

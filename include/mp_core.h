@@ -143,6 +143,12 @@ mp_status mp_framebuffer(mp_ctx* ctx, void** color_dev, void** depth_dev, int32_
 /* Copies layer `view` to host memory; linear != 0 converts to row-major (y up). */
 mp_status mp_read_framebuffer(mp_ctx* ctx, int32_t view, float* color_rgba, int32_t* depth, int32_t linear);
 
+/* Copies layer `view` (tiled colour float4, depth int32) into device buffers on
+ * the context's stream; either pointer may be NULL. */
+mp_status mp_copy_framebuffer_device(mp_ctx* ctx, int32_t view, void* color_dev, void* depth_dev);
+/* Winning micropolygon of every tiled pixel of layer `view` in the last frame:
+ * sub-patch index * reyes_patch_size^2 + nu + nv * reyes_patch_size, or -1. */
+mp_status mp_read_visibility(mp_ctx* ctx, int32_t view, int64_t* ids);
 /* Sub-patches of the last frame, for parity checks: count, then up to cap records
  * (draw index, patch id, range min.x min.y max.x max.y).  Any pointer may be NULL. */
 mp_status mp_subpatches(mp_ctx* ctx, int64_t* count, int32_t* draw, int32_t* pid, float* range, int64_t cap);
@@ -159,6 +165,9 @@ mp_status mp_dice_subpatches(mp_ctx* ctx, int32_t draw, int64_t n, const int32_t
  * Visibility is the last frame's. */
 mp_status mp_set_grad_buffer(mp_ctx* ctx, int32_t draw, void* grad_dev);
 mp_status mp_backward(mp_ctx* ctx, int32_t view, const void* grad_color_dev, void* grad_amp_dev);
+/* Sets the displacement amplitude multiplier (the 0.04/0.02/0.01 amplitudes of
+ * kernels/dice.cl:52-54 are scaled by it) for the following frames. */
+mp_status mp_set_displacement_amplitude(mp_ctx* ctx, float amplitude);
 /* Replaces the control points of a loaded handle in place from device memory (same count). */
 mp_status mp_update_patches_device(mp_ctx* ctx, uint64_t handle, const void* dev_xyz1);
 

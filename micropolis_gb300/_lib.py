@@ -64,11 +64,14 @@ SIGNATURES = [
     ("mp_dump_trace", ctypes.c_int, [c_void_p, ctypes.c_char_p, ctypes.c_size_t]),
     ("mp_framebuffer", ctypes.c_int, [c_void_p, P(c_void_p), P(c_void_p), P(i32), P(i32), P(i32)]),
     ("mp_read_framebuffer", ctypes.c_int, [c_void_p, i32, P(f32), P(i32), i32]),
+    ("mp_copy_framebuffer_device", ctypes.c_int, [c_void_p, i32, c_void_p, c_void_p]),
+    ("mp_read_visibility", ctypes.c_int, [c_void_p, i32, P(i64)]),
     ("mp_subpatches", ctypes.c_int, [c_void_p, P(i64), P(i32), P(i32), P(f32), i64]),
     ("mp_stats_get", ctypes.c_int, [c_void_p, P(MpStats)]),
     ("mp_dice_subpatches", ctypes.c_int, [c_void_p, i32, i64, P(i32), P(f32), P(f32), P(i32), P(f32)]),
     ("mp_set_grad_buffer", ctypes.c_int, [c_void_p, i32, c_void_p]),
     ("mp_backward", ctypes.c_int, [c_void_p, i32, c_void_p, c_void_p]),
+    ("mp_set_displacement_amplitude", ctypes.c_int, [c_void_p, f32]),
     ("mp_update_patches_device", ctypes.c_int, [c_void_p, u64, c_void_p]),
     ("mp_inclusive_scan", ctypes.c_int, [c_void_p, P(i32), P(i32), i64]),
     ("mp_atomic_bench", ctypes.c_int, [c_void_p, i64, i64, i32, P(ctypes.c_double)]),

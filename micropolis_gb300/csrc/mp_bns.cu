@@ -52,10 +52,16 @@ __device__ void set_status(unsigned long long* ctrl, int code) {
     atomicCAS(cw(ctrl, kStatus), 0ull, (unsigned long long)code);
 }
 
+// kQTail packs two counters updated by one atomic: the high 32 bits count
+// queue tickets ever filled (roots included), the low 32 bits the items pushed
+// but not yet finished.  A warp step adds (2*splits << 32) + (2*splits -
+// processed); the borrow of a negative low part is cancelled by the carry.
+constexpr unsigned long long kLow32 = 0xffffffffull;
+
 __global__ void bns_reset_kernel(unsigned long long* ctrl, long long roots) {
-    *cw(ctrl, kQTail) = (unsigned long long)roots;
+    *cw(ctrl, kQTail) = ((unsigned long long)roots << 32) | (unsigned long long)roots;
     *cw(ctrl, kQHead) = 0;
-    *cw(ctrl, kOutstanding) = (unsigned long long)roots;
+    *cw(ctrl, kOutstanding) = 0;
     *cw(ctrl, kOutCount) = 0;
     *cw(ctrl, kDone) = roots == 0 ? 1 : 0;
     *cw(ctrl, kStatus) = 0;
@@ -67,13 +73,24 @@ __global__ void bns_reset_kernel(unsigned long long* ctrl, long long roots) {
 }
 
 constexpr int kBnsBlock = 128;
+constexpr int kBnsSmemDraws = 64;
 constexpr unsigned long long kNoTicket = ~0ull;
 
-__global__ void __launch_bounds__(kBnsBlock) bns_persistent_kernel(const DrawDev* __restrict__ draws,
+__global__ void __launch_bounds__(kBnsBlock) bns_persistent_kernel(const DrawDev* __restrict__ gdraws,
                                                                    const int* __restrict__ root_prefix,
                                                                    int n_draws, FrameDev fr, Queue q,
                                                                    SubPatches out, unsigned long long* ctrl,
                                                                    long long spin_limit) {
+    // draw constants staged in shared memory when they fit
+    __shared__ DrawDev s_draws[kBnsSmemDraws];
+    const bool staged = n_draws <= kBnsSmemDraws;
+    if (staged) {
+        const int words = n_draws * (int)(sizeof(DrawDev) / 4);
+        for (int i = threadIdx.x; i < words; i += blockDim.x)
+            reinterpret_cast<int*>(s_draws)[i] = __ldg(reinterpret_cast<const int*>(gdraws) + i);
+        __syncthreads();
+    }
+    const DrawDev* draws = staged ? s_draws : gdraws;
     const int lane = threadIdx.x & 31;
     const unsigned epoch = (unsigned)*(volatile unsigned long long*)cw(ctrl, kEpoch);
     const unsigned long long R = *(volatile unsigned long long*)cw(ctrl, kRoots);
@@ -157,41 +174,46 @@ __global__ void __launch_bounds__(kBnsBlock) bns_persistent_kernel(const DrawDev
                 }
             }
         }
-        // split children
-        bool split = dec == kSplitX || dec == kSplitY;
-        unsigned smask = __ballot_sync(0xffffffffu, split);
-        int pushed = 0;
-        if (smask) {
-            int leader = __ffs(smask) - 1;
-            unsigned long long base = 0;
-            if (lane == leader) base = atomicAdd(cw(ctrl, kQTail), 2ull * __popc(smask));
-            base = __shfl_sync(0xffffffffu, base, leader);
-            bool fits = false;
-            if (split) {
-                unsigned long long t0 = base + 2ull * __popc(smask & lanemask_lt());
-                unsigned long long s0 = t0 - R;
-                fits = (long long)(s0 + 1) < q.capacity;
-                if (fits) {
-                    float4 c0, c1;
-                    split_children(r, dec, c0, c1);
-                    unsigned meta_y = (unsigned)draw | ((unsigned)(depth + 1) << 24);
-                    q.range[s0] = c0;
-                    q.range[s0 + 1] = c1;
-                    q.meta[s0] = make_uint2((unsigned)pid, meta_y);
-                    q.meta[s0 + 1] = make_uint2((unsigned)pid, meta_y);
-                    __threadfence();
-                    st_release_u32(q.seq + s0, epoch);
-                    st_release_u32(q.seq + s0 + 1, epoch);
-                } else {
-                    set_status(ctrl, kErrOverflow);
-                }
+        // split children: reserve their tickets and account this step's work
+        // with one packed atomic (see kQTail above)
+        const bool split = dec == kSplitX || dec == kSplitY;
+        const unsigned smask = __ballot_sync(0xffffffffu, split);
+        const long long n_child = 2ll * __popc(smask);
+        const long long net = n_child - (long long)__popc(rmask);
+        unsigned long long old = 0;
+        if (lane == 0)
+            old = atomicAdd(cw(ctrl, kQTail), ((unsigned long long)n_child << 32) + (unsigned long long)net);
+        old = __shfl_sync(0xffffffffu, old, 0);
+        bool fits = true;
+        if (split) {
+            const unsigned long long t0 = (old >> 32) + 2ull * __popc(smask & lanemask_lt());
+            const unsigned long long s0 = t0 - R;
+            fits = (long long)(s0 + 1) < q.capacity;
+            if (fits) {
+                float4 c0, c1;
+                split_children(r, dec, c0, c1);
+                const unsigned meta_y = (unsigned)draw | ((unsigned)(depth + 1) << 24);
+                q.range[s0] = c0;
+                q.range[s0 + 1] = c1;
+                q.meta[s0] = make_uint2((unsigned)pid, meta_y);
+                q.meta[s0 + 1] = make_uint2((unsigned)pid, meta_y);
+                // release: the item stores above are visible before the slot's epoch
+                st_release_u32(q.seq + s0, epoch);
+                st_release_u32(q.seq + s0 + 1, epoch);
+            } else {
+                set_status(ctrl, kErrOverflow);
             }
-            pushed = 2 * __popc(__ballot_sync(0xffffffffu, fits));
         }
+        const unsigned lost = __ballot_sync(0xffffffffu, !fits);
         if (lane == 0) {
-            long long delta = (long long)pushed - (long long)__popc(rmask);
-            unsigned long long old = atomicAdd(cw(ctrl, kOutstanding), (unsigned long long)delta);
-            if ((long long)old + delta == 0) st_release_u64(cw(ctrl, kDone), 1ull);
+            long long remaining = (long long)(old & kLow32) + net;
+            if (lost) {
+                // children that found no slot are never processed: take them back
+                const long long back = -2ll * __popc(lost);
+                unsigned long long o2 = atomicAdd(cw(ctrl, kQTail), (unsigned long long)back);
+                remaining = (long long)(o2 & kLow32) + back;
+            }
+            if (remaining == 0) st_release_u64(cw(ctrl, kDone), 1ull);
         }
         if (ready) ticket = kNoTicket;
     }

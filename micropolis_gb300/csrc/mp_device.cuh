@@ -149,6 +149,7 @@ struct RangeBound {
 __device__ __forceinline__ RangeBound bound_range(const DrawDev& d, int pid, float4 r) {
     F3 ps[3][3];
     float sv[3], su[3];
+#pragma unroll
     for (int i = 0; i < 3; ++i) {
         sv[i] = fadd(r.x, fmul(fmul(fsub(r.z, r.x), (float)i), 0.5f));
         su[i] = fadd(r.y, fmul(fmul(fsub(r.w, r.y), (float)i), 0.5f));
@@ -169,9 +170,9 @@ __device__ __forceinline__ RangeBound bound_range(const DrawDev& d, int pid, flo
         }
     } else {
         const float4* P = d.cp + (size_t)pid * 20;
-#pragma unroll 1
+#pragma unroll
         for (int iu = 0; iu < 3; ++iu)
-#pragma unroll 1
+#pragma unroll
             for (int iv = 0; iv < 3; ++iv) ps[iu][iv] = mv_point(d.mv, eval_gregory_cpu(P, su[iv], sv[iu]));
     }
     RangeBound b;
@@ -375,26 +376,36 @@ __device__ __forceinline__ float4 displace(float4 pos, const float* fd) {
 }
 
 // Eye-space position of dice vertex (nu, nv) of a sub-patch (kernels/dice.cl:44-67).
-__device__ __forceinline__ float4 dice_eye(const DrawDev& d, const FrameDev& fr, const float4* P, float4 r,
-                                           int nu, int nv) {
-    float tx = ffma(fsub(r.z, r.x), fdiv((float)nu, (float)fr.PS), r.x);
-    float ty = ffma(fsub(r.w, r.y), fdiv((float)nv, (float)fr.PS), r.y);
-    float4 o = (d.type == 0) ? eval_bezier_dice(P, tx, ty) : eval_gregory_dice(P, tx, ty);
-    float4 pos = mul_m44v4(d.mv, o);
+// nu / PS is exact (PS is a power of two), so it is formed as nu * (1 / PS).
+__device__ __forceinline__ float4 dice_eye_m(int type, const float* mv, const FrameDev& fr, const float4* P,
+                                             float4 r, int nu, int nv) {
+    const float inv = fr.PS == 16 ? 0.0625f : 0.125f;  // 1 / PS, PS in {8, 16}
+    float tx = ffma(fsub(r.z, r.x), fmul((float)nu, inv), r.x);
+    float ty = ffma(fsub(r.w, r.y), fmul((float)nv, inv), r.y);
+    float4 o = (type == 0) ? eval_bezier_dice(P, tx, ty) : eval_gregory_dice(P, tx, ty);
+    float4 pos = mul_m44v4(mv, o);
     if (fr.displacement) pos = displace(pos, fr.fdisp);
     return pos;
 }
+__device__ __forceinline__ float4 dice_eye(const DrawDev& d, const FrameDev& fr, const float4* P, float4 r,
+                                           int nu, int nv) {
+    return dice_eye_m(d.type, d.mv, fr, P, r, nu, nv);
+}
 
 // Projection to fixed-point pixel coordinates and NDC depth (kernels/dice.cl:69-79).
-__device__ __forceinline__ void project_vertex(const DrawDev& d, const FrameDev& fr, float4 pos, int& px, int& py,
-                                               float& depth) {
-    float4 p = mul_m44v4(d.proj, pos);
+__device__ __forceinline__ void project_vertex_m(const float* proj, const FrameDev& fr, float4 pos, int& px,
+                                                 int& py, float& depth) {
+    float4 p = mul_m44v4(proj, pos);
     int vsx = fr.W << fr.shift, vsy = fr.H << fr.shift;
     float ex = fadd(fmul(fmul(fdiv(p.x, p.w), (float)vsx), 0.5f), (float)(vsx / 2));
     float ey = fadd(fmul(fmul(fdiv(p.y, p.w), (float)vsy), 0.5f), (float)(vsy / 2));
     px = __float2int_rz(ex);
     py = __float2int_rz(ey);
     depth = fdiv(p.z, p.w);
+}
+__device__ __forceinline__ void project_vertex(const DrawDev& d, const FrameDev& fr, float4 pos, int& px, int& py,
+                                               float& depth) {
+    project_vertex_m(d.proj, fr, pos, px, py, depth);
 }
 
 struct V3 { float x, y, z; };
@@ -407,21 +418,38 @@ __device__ __forceinline__ V3 normalize3(V3 v) {
     return V3{fdiv(v.x, l), fdiv(v.y, l), fdiv(v.z, l)};
 }
 
-// kernels/reyes.cl:172-191 -- flat colour of a quad from its 4 eye positions
-// (vertex order 0:(u,v) 1:(u+1,v) 2:(u,v+1) 3:(u+1,v+1)); the specular term
-// has colour 0 and contributes +0.
-__device__ __forceinline__ float4 shade_quad(const float4* pos, const float* dc) {
-    V3 du{fmul(fsub(fadd(fsub(pos[1].x, pos[0].x), pos[3].x), pos[2].x), 0.5f),
-          fmul(fsub(fadd(fsub(pos[1].y, pos[0].y), pos[3].y), pos[2].y), 0.5f),
-          fmul(fsub(fadd(fsub(pos[1].z, pos[0].z), pos[3].z), pos[2].z), 0.5f)};
-    V3 dv{fmul(fsub(fadd(fsub(pos[2].x, pos[0].x), pos[3].x), pos[1].x), 0.5f),
-          fmul(fsub(fadd(fsub(pos[2].y, pos[0].y), pos[3].y), pos[1].y), 0.5f),
-          fmul(fsub(fadd(fsub(pos[2].z, pos[0].z), pos[3].z), pos[1].z), 0.5f)};
+// kernels/reyes.cl:172-191 -- flat shading of a quad from its 4 eye positions
+// (vertex order 0:(u,v) 1:(u+1,v) 2:(u,v+1) 3:(u+1,v+1)).  shade_m is the
+// diffuse factor max(dot(n, l), 0); shade_color the colour
+// ac*dc + m*dc + pow(..)*sc with sc = 0, whose last term is +0.
+__device__ __forceinline__ V3 light_dir() { return normalize3(V3{4.0f, 3.0f, 8.0f}); }
+__device__ __forceinline__ float shade_m_l(V3 l, float x0, float y0, float z0, float x1, float y1, float z1,
+                                           float x2, float y2, float z2, float x3, float y3, float z3) {
+    V3 du{fmul(fsub(fadd(fsub(x1, x0), x3), x2), 0.5f), fmul(fsub(fadd(fsub(y1, y0), y3), y2), 0.5f),
+          fmul(fsub(fadd(fsub(z1, z0), z3), z2), 0.5f)};
+    V3 dv{fmul(fsub(fadd(fsub(x2, x0), x3), x1), 0.5f), fmul(fsub(fadd(fsub(y2, y0), y3), y1), 0.5f),
+          fmul(fsub(fadd(fsub(z2, z0), z3), z1), 0.5f)};
+    V3 n = normalize3(cross3(dv, du));
+    return fmaxf(dot3(n, l), 0.0f);
+}
+__device__ __forceinline__ float shade_m(float x0, float y0, float z0, float x1, float y1, float z1, float x2,
+                                         float y2, float z2, float x3, float y3, float z3) {
+    V3 du{fmul(fsub(fadd(fsub(x1, x0), x3), x2), 0.5f), fmul(fsub(fadd(fsub(y1, y0), y3), y2), 0.5f),
+          fmul(fsub(fadd(fsub(z1, z0), z3), z2), 0.5f)};
+    V3 dv{fmul(fsub(fadd(fsub(x2, x0), x3), x1), 0.5f), fmul(fsub(fadd(fsub(y2, y0), y3), y1), 0.5f),
+          fmul(fsub(fadd(fsub(z2, z0), z3), z1), 0.5f)};
     V3 n = normalize3(cross3(dv, du));
     V3 l = normalize3(V3{4.0f, 3.0f, 8.0f});
-    float m = fmaxf(dot3(n, l), 0.0f);
+    return fmaxf(dot3(n, l), 0.0f);
+}
+__device__ __forceinline__ float4 shade_color(float m, const float* dc) {
     return make_float4(fadd(ffma(m, dc[0], fmul(0.015f, dc[0])), 0.0f), fadd(ffma(m, dc[1], fmul(0.015f, dc[1])), 0.0f),
                        fadd(ffma(m, dc[2], fmul(0.015f, dc[2])), 0.0f), fadd(ffma(m, dc[3], fmul(1.0f, dc[3])), 0.0f));
+}
+__device__ __forceinline__ float4 shade_quad(const float4* pos, const float* dc) {
+    return shade_color(shade_m(pos[0].x, pos[0].y, pos[0].z, pos[1].x, pos[1].y, pos[1].z, pos[2].x, pos[2].y,
+                               pos[2].z, pos[3].x, pos[3].y, pos[3].z),
+                       dc);
 }
 
 // kernels/reyes.cl:240-265 edge setup of one triangle (wrapping int32, R5).

@@ -64,6 +64,8 @@ struct mp_ctx {
     SubPatches sub{};
     BigQuad* big = nullptr;
     long long big_cap = 0;
+    float* mshade = nullptr;          // diffuse factor per micropolygon (batched path)
+    long long mshade_cap = 0;
     Framebuffer fb{};
 
     // plain path
@@ -84,11 +86,13 @@ struct mp_ctx {
     cudaGraphExec_t graph = nullptr;
     int graph_draws = -1;
     long long graph_roots = -1;
-    const void* graph_key[4] = {nullptr, nullptr, nullptr, nullptr};
+    const void* graph_key[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
 
     int bns_grid = 0, raster_grid = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     bool stage_timing = false;
+    void* staging = nullptr;          // pinned upload buffer
+    size_t staging_bytes = 0;
     cudaEvent_t sev[8] = {};
     mp_stats stats{};
     long long plain_bounds = 0, plain_passes = 0, plain_out = 0;
@@ -137,8 +141,9 @@ void perspective(float fovy_rad, float aspect, float zn, float zf, float* m) {
     m[14] = -(2.0f * zf * zn) / (zf - zn);
 }
 
-long long auto_queue_cap(long long roots) { return std::max(1LL << 20, roots * 48); }
-long long auto_sub_cap(long long roots) { return std::max(1LL << 19, roots * 32); }
+// first-frame guesses; both grow (and the frame is rendered again) on overflow
+long long auto_queue_cap(long long roots) { return std::min(std::max(1LL << 22, roots * 640), 1LL << 28); }
+long long auto_sub_cap(long long roots) { return std::min(std::max(1LL << 20, roots * 320), 1LL << 26); }
 
 mp_status grow_queue(mp_ctx* c, long long need) {
     if (need <= c->q.capacity) return MP_OK;
@@ -184,6 +189,17 @@ mp_status grow_big(mp_ctx* c, long long need) {
     c->big = nullptr;
     CK(dalloc(&c->big, cap));
     c->big_cap = cap;
+    return MP_OK;
+}
+
+mp_status ensure_mshade(mp_ctx* c) {
+    const long long need = c->sub.capacity * c->fr.PS * c->fr.PS;
+    if (need <= c->mshade_cap) return MP_OK;
+    dfree(c->mshade);
+    c->mshade = nullptr;
+    c->mshade_cap = 0;
+    CK(dalloc(&c->mshade, need));
+    c->mshade_cap = need;
     return MP_OK;
 }
 
@@ -364,9 +380,10 @@ mp_status capture_frame(mp_ctx* c, int n, long long roots) {
     launch_clear(c->fb, c->fr, 0, c->stream);
     launch_bns_persistent(c->d_draws, c->d_root_prefix, n, c->fr, c->q, c->sub, c->ctrl, c->bns_grid,
                           c->opt.spin_limit, c->stream);
-    launch_raster_fused(c->d_draws, c->fr, c->sub, c->fb, c->big, c->big_cap, c->ctrl, c->raster_grid, c->stream);
+    launch_raster_fused(c->d_draws, c->fr, c->sub, c->fb, c->mshade, c->big, c->big_cap, c->ctrl, c->raster_grid,
+                        c->stream);
     launch_raster_big(c->d_draws, c->fr, c->fb, c->big, c->big_cap, c->ctrl, c->stream);
-    launch_resolve(c->d_draws, c->fr, c->sub, c->fb, c->stream);
+    launch_resolve(c->d_draws, c->fr, c->sub, c->fb, c->mshade, c->stream);
     cudaMemcpyAsync(c->h_ctrl, c->ctrl, sizeof(unsigned long long) * kNumCtrl * kCtrlStride, cudaMemcpyDeviceToHost,
                     c->stream);
     cudaError_t e = cudaStreamEndCapture(c->stream, &g);
@@ -380,6 +397,7 @@ mp_status capture_frame(mp_ctx* c, int n, long long roots) {
     c->graph_key[1] = c->sub.range;
     c->graph_key[2] = c->big;
     c->graph_key[3] = c->d_draws;
+    c->graph_key[4] = c->mshade;
     return MP_OK;
 }
 
@@ -398,7 +416,9 @@ mp_status batched_frame(mp_ctx* c) {
     if (roots >= (1LL << 31)) return fail(c, MP_ERR_INVALID_ARG, "more than 2^31 patches in one frame");
     long long qcap = c->opt.queue_capacity > 0 ? c->opt.queue_capacity : auto_queue_cap(roots);
     long long scap = c->opt.subpatch_capacity > 0 ? c->opt.subpatch_capacity : auto_sub_cap(roots);
-    if ((st = grow_queue(c, qcap)) || (st = grow_sub(c, scap, false)) || (st = grow_big(c, 1 << 16))) return st;
+    if ((st = grow_queue(c, qcap)) || (st = grow_sub(c, scap, false)) || (st = grow_big(c, 1 << 16)) ||
+        (st = ensure_mshade(c)))
+        return st;
     for (int attempt = 0; attempt < 8; ++attempt) {
         if (c->stage_timing) {
             // the same launches as the graph, with an event after each stage
@@ -412,12 +432,12 @@ mp_status batched_frame(mp_ctx* c) {
             launch_bns_persistent(c->d_draws, c->d_root_prefix, n, c->fr, c->q, c->sub, c->ctrl, c->bns_grid,
                                   c->opt.spin_limit, c->stream);
             CK(cudaEventRecord(c->sev[1], c->stream));
-            launch_raster_fused(c->d_draws, c->fr, c->sub, c->fb, c->big, c->big_cap, c->ctrl, c->raster_grid,
-                                c->stream);
+            launch_raster_fused(c->d_draws, c->fr, c->sub, c->fb, c->mshade, c->big, c->big_cap, c->ctrl,
+                                c->raster_grid, c->stream);
             CK(cudaEventRecord(c->sev[2], c->stream));
             launch_raster_big(c->d_draws, c->fr, c->fb, c->big, c->big_cap, c->ctrl, c->stream);
             CK(cudaEventRecord(c->sev[3], c->stream));
-            launch_resolve(c->d_draws, c->fr, c->sub, c->fb, c->stream);
+            launch_resolve(c->d_draws, c->fr, c->sub, c->fb, c->mshade, c->stream);
             CK(cudaEventRecord(c->sev[4], c->stream));
             CK(cudaEventRecord(c->ev1, c->stream));
             CK(cudaMemcpyAsync(c->h_ctrl, c->ctrl, sizeof(unsigned long long) * kNumCtrl * kCtrlStride,
@@ -433,7 +453,8 @@ mp_status batched_frame(mp_ctx* c) {
             }
         } else {
         if (!c->graph || c->graph_draws != n || c->graph_roots != roots || c->graph_key[0] != c->q.range ||
-            c->graph_key[1] != c->sub.range || c->graph_key[2] != c->big || c->graph_key[3] != c->d_draws) {
+            c->graph_key[1] != c->sub.range || c->graph_key[2] != c->big || c->graph_key[3] != c->d_draws ||
+            c->graph_key[4] != c->mshade) {
             st = capture_frame(c, n, roots);
             if (st) return st;
         }
@@ -448,11 +469,12 @@ mp_status batched_frame(mp_ctx* c) {
             break;
         }
         // regrow what overflowed and render the frame again
-        long long pushed = (long long)hc(c, kQTail) - roots;
+        long long pushed = (long long)(hc(c, kQTail) >> 32) - roots;
         long long outc = (long long)hc(c, kOutCount);
         long long bigc = (long long)hc(c, kBigCount);
         if (pushed > c->q.capacity && (st = grow_queue(c, pushed + pushed / 2))) return st;
-        if (outc > c->sub.capacity && (st = grow_sub(c, outc + outc / 4, false))) return st;
+        if (outc > c->sub.capacity && ((st = grow_sub(c, outc + outc / 4, false)) || (st = ensure_mshade(c))))
+            return st;
         if (bigc > c->big_cap && (st = grow_big(c, bigc * 2))) return st;
         if (attempt == 7) return fail(c, MP_ERR_OVERFLOW, "capacity still exceeded after regrowth");
     }
@@ -615,6 +637,7 @@ void mp_destroy(mp_ctx* c) {
     for (auto& kv : c->meshes) dfree(kv.second.cp);
     dfree(c->ctrl);
     if (c->h_ctrl) cudaFreeHost(c->h_ctrl);
+    if (c->staging) cudaFreeHost(c->staging);
     dfree(c->d_draws);
     dfree(c->d_root_prefix);
     if (c->h_draws) cudaFreeHost(c->h_draws);
@@ -622,6 +645,7 @@ void mp_destroy(mp_ctx* c) {
     dfree(c->q.range); dfree(c->q.meta); dfree(c->q.seq);
     dfree(c->sub.range); dfree(c->sub.meta);
     dfree(c->big);
+    dfree(c->mshade);
     dfree(c->fb.keys); dfree(c->fb.color); dfree(c->fb.depth);
     dfree(c->stack.range); dfree(c->stack.meta);
     dfree(c->pad_range); dfree(c->pad_meta); dfree(c->dec); dfree(c->keys); dfree(c->scan_state);
@@ -656,37 +680,52 @@ static mp_status load_common(mp_ctx* c, uint64_t handle, const void* src, size_t
     if (!c) return MP_ERR_INVALID_ARG;
     // Scene::draw loads on first use inside a frame (src/micropolis/Scene.cpp:186-188);
     // only replacing a handle that this frame may already reference is refused
-    if (c->in_frame && c->meshes.count(handle))
-        return fail(c, MP_ERR_STATE, "reloading a handle inside a frame");
+    if (c->in_frame && c->meshes.count(handle) && !c->draws.empty())
+        return fail(c, MP_ERR_STATE, "reloading a handle after this frame's first draw");
     if (type != MP_BEZIER && type != MP_GREGORY) return fail(c, MP_ERR_INVALID_ARG, "bad patch type");
     const size_t per = type == MP_BEZIER ? 16 : 20;
     if (n_points % per) return fail(c, MP_ERR_INVALID_ARG, "point count is not a whole number of patches");
     if (n_points / per >= (1u << 31)) return fail(c, MP_ERR_INVALID_ARG, "too many patches");
     if (n_points && !src) return fail(c, MP_ERR_INVALID_ARG, "null patch data");
-    auto it = c->meshes.find(handle);
-    if (it != c->meshes.end()) {
-        dfree(it->second.cp);
-        c->meshes.erase(it);
-    }
     Mesh m;
-    m.n_patches = (int)(n_points / per);
-    m.type = type;
-    m.n_points = n_points;
-    CK(dalloc(&m.cp, (long long)n_points));
+    auto it = c->meshes.find(handle);
+    if (it != c->meshes.end() && it->second.n_points == n_points && it->second.type == type) {
+        m = it->second;  // same size: reuse the device buffer
+    } else {
+        if (it != c->meshes.end()) {
+            CK(cudaStreamSynchronize(c->stream));
+            dfree(it->second.cp);
+            c->meshes.erase(it);
+        }
+        m.n_patches = (int)(n_points / per);
+        m.type = type;
+        m.n_points = n_points;
+        CK(dalloc(&m.cp, (long long)n_points));
+    }
     if (n_points) {
         if (device) {
             CK(cudaMemcpyAsync(m.cp, src, sizeof(float4) * n_points, cudaMemcpyDeviceToDevice, c->stream));
         } else {
-            // src/Reyes/PatchIndex.cpp:83-98: widen vec3 to (x, y, z, 1) and upload
-            std::vector<float4> tmp(n_points);
+            // src/Reyes/PatchIndex.cpp:83-98: widen vec3 to (x, y, z, 1) and upload,
+            // through a pinned staging buffer reused across loads
+            if (c->staging_bytes < sizeof(float4) * n_points) {
+                CK(cudaStreamSynchronize(c->stream));
+                if (c->staging) cudaFreeHost(c->staging);
+                c->staging = nullptr;
+                c->staging_bytes = 0;
+                CK(cudaMallocHost(&c->staging, sizeof(float4) * n_points));
+                c->staging_bytes = sizeof(float4) * n_points;
+            } else {
+                CK(cudaStreamSynchronize(c->stream));  // the previous upload has left the staging buffer
+            }
+            float4* tmp = (float4*)c->staging;
             const float* f = (const float*)src;
             for (size_t i = 0; i < n_points; ++i) tmp[i] = make_float4(f[3 * i], f[3 * i + 1], f[3 * i + 2], 1.0f);
-            CK(cudaMemcpyAsync(m.cp, tmp.data(), sizeof(float4) * n_points, cudaMemcpyHostToDevice, c->stream));
+            CK(cudaMemcpyAsync(m.cp, tmp, sizeof(float4) * n_points, cudaMemcpyHostToDevice, c->stream));
         }
-        CK(cudaStreamSynchronize(c->stream));
+        if (!c->in_frame) CK(cudaStreamSynchronize(c->stream));
     }
     c->meshes[handle] = m;
-    invalidate_graph(c);
     return MP_OK;
 }
 
@@ -697,6 +736,17 @@ mp_status mp_load_patches(mp_ctx* c, uint64_t handle, const float* xyz, size_t n
 mp_status mp_load_patches_device(mp_ctx* c, uint64_t handle, const void* dev_xyz1, size_t n_points,
                                  mp_patch_type type) {
     return load_common(c, handle, dev_xyz1, n_points, type, true);
+}
+
+mp_status mp_set_displacement_amplitude(mp_ctx* c, float amp) {
+    if (!c || !std::isfinite(amp)) return MP_ERR_INVALID_ARG;
+    if (c->in_frame) return fail(c, MP_ERR_STATE, "amplitude change inside a frame");
+    c->opt.displacement_amplitude = amp;
+    c->fr.fdisp[0] = 0.04f * amp;
+    c->fr.fdisp[1] = 0.02f * amp;
+    c->fr.fdisp[2] = 0.01f * amp;
+    invalidate_graph(c);  // the frame constants are kernel parameters of the graph
+    return MP_OK;
 }
 
 mp_status mp_update_patches_device(mp_ctx* c, uint64_t handle, const void* dev_xyz1) {
@@ -771,7 +821,7 @@ mp_status mp_finish(mp_ctx* c) {
         st = batched_frame(c);
         if (st) return st;
         c->stats.subpatches = std::min((long long)hc(c, kOutCount), c->sub.capacity);
-        c->stats.bounds = (long long)hc(c, kQTail);
+        c->stats.bounds = (long long)(hc(c, kQTail) >> 32);
         c->stats.passes = 1;
     } else {
         CK(cudaEventRecord(c->ev1, c->stream));
@@ -840,6 +890,31 @@ mp_status mp_read_framebuffer(mp_ctx* c, int32_t view, float* color, int32_t* de
     if (ddst) CK(cudaMemcpyAsync(ddst, c->fb.depth + view * n, sizeof(int) * (size_t)n, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     if (linear) untile(cdst, ddst, color, depth, c->fr.W, c->fr.H);
+    return MP_OK;
+}
+
+mp_status mp_copy_framebuffer_device(mp_ctx* c, int32_t view, void* color_dev, void* depth_dev) {
+    if (!c || view < 0 || view >= c->fb.views) return MP_ERR_INVALID_ARG;
+    const long long n = c->fb.pixels;
+    if (color_dev)
+        CK(cudaMemcpyAsync(color_dev, c->fb.color + view * n, sizeof(float4) * (size_t)n, cudaMemcpyDeviceToDevice,
+                           c->stream));
+    if (depth_dev)
+        CK(cudaMemcpyAsync(depth_dev, c->fb.depth + view * n, sizeof(int) * (size_t)n, cudaMemcpyDeviceToDevice,
+                           c->stream));
+    return MP_OK;
+}
+
+mp_status mp_read_visibility(mp_ctx* c, int32_t view, int64_t* ids) {
+    if (!c || !ids || view < 0 || view >= c->fb.views) return MP_ERR_INVALID_ARG;
+    if (!c->frame_valid) return fail(c, MP_ERR_STATE, "no finished frame");
+    const long long n = c->fb.pixels;
+    std::vector<unsigned long long> k((size_t)n);
+    CK(cudaMemcpyAsync(k.data(), c->fb.keys + view * n, sizeof(unsigned long long) * (size_t)n,
+                       cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    for (long long i = 0; i < n; ++i)
+        ids[i] = k[(size_t)i] == kClearKey ? -1 : (int64_t)(k[(size_t)i] & 0xffffffffull);
     return MP_OK;
 }
 

@@ -81,12 +81,13 @@ long long scan_state_words(long long n);
 // ---- dice / shade / raster / resolve (mp_raster.cu)
 void launch_clear(const Framebuffer& fb, const FrameDev& fr, int with_color, cudaStream_t s);
 void launch_raster_fused(const DrawDev* draws, const FrameDev& fr, const SubPatches& sub, const Framebuffer& fb,
-                         BigQuad* big, long long big_cap, unsigned long long* ctrl, int grid, cudaStream_t s);
+                         float* mshade, BigQuad* big, long long big_cap, unsigned long long* ctrl, int grid,
+                         cudaStream_t s);
 int raster_fused_grid(int PS);
 void launch_raster_big(const DrawDev* draws, const FrameDev& fr, const Framebuffer& fb, const BigQuad* big,
                        long long big_cap, unsigned long long* ctrl, cudaStream_t s);
 void launch_resolve(const DrawDev* draws, const FrameDev& fr, const SubPatches& sub, const Framebuffer& fb,
-                    cudaStream_t s);
+                    const float* mshade, cudaStream_t s);
 // plain per-pass path
 void launch_dice_grid(const DrawDev* draws, const FrameDev& fr, const SubPatches& sub, long long base, int count,
                       float4* pos, int2* pxl, float* depth, cudaStream_t s);

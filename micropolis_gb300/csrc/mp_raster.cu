@@ -139,118 +139,154 @@ __device__ __forceinline__ void push_big(BigQuad* big, long long big_cap, unsign
     big[i] = b;
 }
 
-constexpr int kRasterWarps = 8;
+// The fused kernel works on groups of NS sub-patches per 256-thread block:
+// NS * (PS+1)^2 dice vertices are spread over all threads (22 * 81 = 1782 =
+// 7 rounds of 256 at PS = 8), then the block bounds, then one thread per quad.
+constexpr int kFusedThreads = 256;
+template <int PS> struct FusedCfg;
+template <> struct FusedCfg<8> { static constexpr int NS = 22; static constexpr int MINB = 3; };
+template <> struct FusedCfg<16> { static constexpr int NS = 6; static constexpr int MINB = 3; };
 
 template <int PS>
-struct RasterSmem {
-    float4 cp[kRasterWarps][20];
-    int2 pxl[kRasterWarps][(PS + 1) * (PS + 1)];
-    float dep[kRasterWarps][(PS + 1) * (PS + 1)];
+struct FusedSmem {
+    static constexpr int NS = FusedCfg<PS>::NS, G = PS + 1, NV = G * G, NB = (PS / 8) * (PS / 8);
+    float4 cp[NS][20];
+    float mv[NS][16];
+    float proj[NS][16];
+    float4 range[NS];
+    int2 meta[NS];
+    int type[NS], view[NS];
+    int bound[NS][NB][4];
+    unsigned zero[NS];
+    int px[NS * NV], py[NS * NV];
+    float dep[NS * NV];
+    float ex[NS * NV], ey[NS * NV], ez[NS * NV];
 };
 
 template <int PS>
-__global__ void __launch_bounds__(kRasterWarps * 32) raster_fused_kernel(const DrawDev* __restrict__ draws,
-                                                                        FrameDev fr, SubPatches sub,
-                                                                        Framebuffer fb, BigQuad* big,
-                                                                        long long big_cap,
-                                                                        unsigned long long* ctrl) {
-    constexpr int G = PS + 1, NV = G * G, NQ = PS * PS, BPL = PS / 8, NB = BPL * BPL;
-    __shared__ RasterSmem<PS> sm;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+__global__ void __launch_bounds__(kFusedThreads, FusedCfg<PS>::MINB)
+    raster_fused_kernel(const DrawDev* __restrict__ draws, FrameDev fr, SubPatches sub, Framebuffer fb,
+                        float* __restrict__ mshade, BigQuad* big, long long big_cap, unsigned long long* ctrl) {
+    using SM = FusedSmem<PS>;
+    constexpr int NS = SM::NS, G = SM::G, NV = SM::NV, NQ = PS * PS, BPL = PS / 8, NB = SM::NB;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    SM& sm = *reinterpret_cast<SM*>(smem_raw);
+    const int tid = threadIdx.x;
     long long S = (long long)*(volatile unsigned long long*)cw(ctrl, kOutCount);
     if (S > sub.capacity) S = sub.capacity;
+    const int vmaxx = (fr.W << fr.shift) - 1, vmaxy = (fr.H << fr.shift) - 1;
+    const V3 light = light_dir();
     long long frags = 0;
-    const long long nwarps = (long long)gridDim.x * kRasterWarps;
-    for (long long s = (long long)blockIdx.x * kRasterWarps + warp; s < S; s += nwarps) {
-        const float4 r = sub.range[s];
-        const int2 m = sub.meta[s];
-        const DrawDev& d = draws[m.y];
-        const int ncp = d.type == 0 ? 16 : 20;
-        if (lane < ncp) sm.cp[warp][lane] = __ldg(d.cp + (size_t)m.x * ncp + lane);
-        __syncwarp();
-        unsigned zblocks = 0;
-        for (int v = lane; v < NV; v += 32) {
-            int nu = v % G, nv = v / G;
-            float4 pos = dice_eye(d, fr, sm.cp[warp], r, nu, nv);
+    for (long long base = (long long)blockIdx.x * NS; base < S; base += (long long)gridDim.x * NS) {
+        const int n = (int)min((long long)NS, S - base);
+        if (tid < n) {
+            sm.range[tid] = sub.range[base + tid];
+            sm.meta[tid] = sub.meta[base + tid];
+            sm.zero[tid] = 0;
+        }
+        for (int i = tid; i < n * NB; i += kFusedThreads) {
+            int* b = sm.bound[i / NB][i % NB];
+            b[0] = vmaxx; b[1] = vmaxy; b[2] = 0; b[3] = 0;
+        }
+        __syncthreads();
+        for (int i = tid; i < n * 20; i += kFusedThreads) {
+            const int k = i / 20, c = i % 20;
+            const DrawDev& d = draws[sm.meta[k].y];
+            const int ncp = d.type == 0 ? 16 : 20;
+            if (c < ncp) sm.cp[k][c] = __ldg(d.cp + (size_t)sm.meta[k].x * ncp + c);
+        }
+        for (int i = tid; i < n * 32; i += kFusedThreads) {
+            const int k = i >> 5, c = i & 31;
+            const DrawDev& d = draws[sm.meta[k].y];
+            if (c < 16) sm.mv[k][c] = d.mv[c]; else sm.proj[k][c - 16] = d.proj[c - 16];
+            if (c == 0) { sm.type[k] = d.type; sm.view[k] = d.view; }
+        }
+        __syncthreads();
+        // dice vertices (kernels/dice.cl:37-80)
+        for (int i = tid; i < n * NV; i += kFusedThreads) {
+            const int k = i / NV, v = i % NV;
+            const int nu = v % G, nv = v / G;
+            float4 pos = dice_eye_m(sm.type[k], sm.mv[k], fr, sm.cp[k], sm.range[k], nu, nv);
             int px, py;
             float dep;
-            project_vertex(d, fr, pos, px, py, dep);
-            sm.pxl[warp][v] = make_int2(px, py);
-            sm.dep[warp][v] = dep;
+            project_vertex_m(sm.proj[k], fr, pos, px, py, dep);
+            sm.px[i] = px;
+            sm.py[i] = py;
+            sm.dep[i] = dep;
+            sm.ex[i] = pos.x;
+            sm.ey[i] = pos.y;
+            sm.ez[i] = pos.z;
             if (pos.z == 0.0f) {
-                // the vertex belongs to the quads (nu-1..nu, nv-1..nv)
+                // a vertex at eye z == 0 drops every 8x8 block it belongs to (kernels/reyes.cl:130-162)
+                unsigned zb = 0;
                 for (int bv = max(nv - 1, 0) / 8; bv <= min(nv, PS - 1) / 8; ++bv)
-                    for (int bu = max(nu - 1, 0) / 8; bu <= min(nu, PS - 1) / 8; ++bu) zblocks |= 1u << (bu + bv * BPL);
+                    for (int bu = max(nu - 1, 0) / 8; bu <= min(nu, PS - 1) / 8; ++bu) zb |= 1u << (bu + bv * BPL);
+                atomicOr(&sm.zero[k], zb);
             }
         }
-        zblocks = __reduce_or_sync(0xffffffffu, zblocks);
-        __syncwarp();
+        __syncthreads();
         // block bounds over front-facing quads (kernels/reyes.cl:120-166)
-        int bxmin[NB], bymin[NB], bxmax[NB], bymax[NB];
-        const int vmaxx = (fr.W << fr.shift) - 1, vmaxy = (fr.H << fr.shift) - 1;
-#pragma unroll
-        for (int b = 0; b < NB; ++b) { bxmin[b] = vmaxx; bymin[b] = vmaxy; bxmax[b] = 0; bymax[b] = 0; }
-        for (int q = lane; q < NQ; q += 32) {
-            int nu = q % PS, nv = q / PS, i0 = nu + nv * G;
-            int qx[4], qy[4];
-            int2 a = sm.pxl[warp][i0], b1 = sm.pxl[warp][i0 + 1], c = sm.pxl[warp][i0 + G], e = sm.pxl[warp][i0 + G + 1];
-            qx[0] = a.x; qy[0] = a.y; qx[1] = b1.x; qy[1] = b1.y; qx[2] = c.x; qy[2] = c.y; qx[3] = e.x; qy[3] = e.y;
+        for (int i = tid; i < n * NQ; i += kFusedThreads) {
+            const int k = i / NQ, q = i % NQ;
+            const int nu = q % PS, nv = q / PS, i0 = k * NV + nu + nv * G;
+            const int qx[4] = {sm.px[i0], sm.px[i0 + 1], sm.px[i0 + G], sm.px[i0 + G + 1]};
+            const int qy[4] = {sm.py[i0], sm.py[i0 + 1], sm.py[i0 + G], sm.py[i0 + G + 1]};
             QuadBound qb = quad_block_bound(fr, qx, qy);
-            if (qb.ff) {
-                int blk = (nu >> 3) + (nv >> 3) * BPL;
-#pragma unroll
-                for (int b = 0; b < NB; ++b)
-                    if (b == blk) {
-                        bxmin[b] = min(bxmin[b], qb.pminx);
-                        bymin[b] = min(bymin[b], qb.pminy);
-                        bxmax[b] = max(bxmax[b], qb.pmaxx);
-                        bymax[b] = max(bymax[b], qb.pmaxy);
-                    }
+            if (!qb.ff) { qb.pminx = vmaxx; qb.pminy = vmaxy; qb.pmaxx = 0; qb.pmaxy = 0; }
+            // lanes of one (sub-patch, block) reduce in registers, then one
+            // shared atomic per group (n * NQ is a multiple of 32: whole warps)
+            const unsigned grp = __match_any_sync(0xffffffffu, k * NB + (nu >> 3) + (nv >> 3) * BPL);
+            const int x0 = __reduce_min_sync(grp, qb.pminx), y0 = __reduce_min_sync(grp, qb.pminy);
+            const int x1 = __reduce_max_sync(grp, qb.pmaxx), y1 = __reduce_max_sync(grp, qb.pmaxy);
+            if ((tid & 31) == __ffs(grp) - 1) {
+                int* b = sm.bound[k][(nu >> 3) + (nv >> 3) * BPL];
+                atomicMin(b + 0, x0);
+                atomicMin(b + 1, y0);
+                atomicMax(b + 2, x1);
+                atomicMax(b + 3, y1);
             }
         }
-        int tiles[NB][4];
-        unsigned live = 0;
+        __syncthreads();
+        // rasterize every quad of a live block
+        for (int i = tid; i < n * NQ; i += kFusedThreads) {
+            const int k = i / NQ, q = i % NQ;
+            const int nu = q % PS, nv = q / PS, blk = (nu >> 3) + (nv >> 3) * BPL;
+            const int* bb = sm.bound[k][blk];
+            int tiles[4];
+            if (!block_tiles(fr, bb[0], bb[1], bb[2], bb[3], !((sm.zero[k] >> blk) & 1), tiles)) continue;
+            const int i0 = k * NV + nu + nv * G;
+            const int idx[4] = {i0, i0 + 1, i0 + G, i0 + G + 1};
+            int qx[4], qy[4];
+            float qd[4];
 #pragma unroll
-        for (int b = 0; b < NB; ++b) {
-            int x0 = __reduce_min_sync(0xffffffffu, bxmin[b]);
-            int y0 = __reduce_min_sync(0xffffffffu, bymin[b]);
-            int x1 = __reduce_max_sync(0xffffffffu, bxmax[b]);
-            int y1 = __reduce_max_sync(0xffffffffu, bymax[b]);
-            if (block_tiles(fr, x0, y0, x1, y1, !((zblocks >> b) & 1), tiles[b])) live |= 1u << b;
-        }
-        if (live) {
-            unsigned long long* keys = fb.keys + (long long)d.view * fb.pixels;
-            for (int q = lane; q < NQ; q += 32) {
-                int nu = q % PS, nv = q / PS, blk = (nu >> 3) + (nv >> 3) * BPL;
-                if (!((live >> blk) & 1)) continue;
-                int i0 = nu + nv * G;
-                const int idx[4] = {i0, i0 + 1, i0 + G, i0 + G + 1};
-                int qx[4], qy[4];
-                float qd[4];
-#pragma unroll
-                for (int k = 0; k < 4; ++k) {
-                    int2 p = sm.pxl[warp][idx[k]];
-                    qx[k] = p.x;
-                    qy[k] = p.y;
-                    qd[k] = sm.dep[warp][idx[k]];
-                }
-                unsigned mp_id = (unsigned)(s * NQ + nu + nv * PS);
-                int minx, miny, maxx, maxy;
-                if (quad_is_fast(qx, qy, minx, miny, maxx, maxy)) {
-                    frags += raster_quad_fast(fr, keys, qx, qy, qd, minx, miny, maxx, maxy, mp_id);
-                } else {
-                    int t4[4];
-#pragma unroll
-                    for (int b = 0; b < NB; ++b)
-                        if (b == blk) { t4[0] = tiles[b][0]; t4[1] = tiles[b][1]; t4[2] = tiles[b][2]; t4[3] = tiles[b][3]; }
-                    push_big(big, big_cap, ctrl, qx, qy, qd, mp_id, d.view, t4);
-                }
+            for (int c = 0; c < 4; ++c) {
+                qx[c] = sm.px[idx[c]];
+                qy[c] = sm.py[idx[c]];
+                qd[c] = sm.dep[idx[c]];
             }
+            const long long s = base + k;
+            const unsigned mp_id = (unsigned)(s * NQ + nu + nv * PS);
+            const int view = sm.view[k];
+            unsigned long long* keys = fb.keys + (long long)view * fb.pixels;
+            int minx, miny, maxx, maxy, f = 0;
+            const bool fast = quad_is_fast(qx, qy, minx, miny, maxx, maxy);
+            if (fast)
+                f = raster_quad_fast(fr, keys, qx, qy, qd, minx, miny, maxx, maxy, mp_id);
+            else
+                push_big(big, big_cap, ctrl, qx, qy, qd, mp_id, view, tiles);
+            if (f > 0 || !fast) {
+                // the diffuse factor of a quad that may own pixels; resolve
+                // turns it into the colour of kernels/reyes.cl:191
+                mshade[mp_id] = shade_m_l(light, sm.ex[idx[0]], sm.ey[idx[0]], sm.ez[idx[0]], sm.ex[idx[1]], sm.ey[idx[1]],
+                                        sm.ez[idx[1]], sm.ex[idx[2]], sm.ey[idx[2]], sm.ez[idx[2]], sm.ex[idx[3]],
+                                        sm.ey[idx[3]], sm.ez[idx[3]]);
+            }
+            frags += f;
         }
-        __syncwarp();
+        __syncthreads();
     }
     frags = __reduce_add_sync(0xffffffffu, (unsigned)frags);
-    if (lane == 0 && frags) atomicAdd(cw(ctrl, kFragments), (unsigned long long)frags);
+    if ((tid & 31) == 0 && frags) atomicAdd(cw(ctrl, kFragments), (unsigned long long)frags);
 }
 
 // Exact replay of the reference's per-tile candidate loop for one quad
@@ -336,24 +372,12 @@ __global__ void clear_kernel(Framebuffer fb, FrameDev fr, int with_color) {
     }
 }
 
-// Colour of micropolygon `id` recomputed from its sub-patch record.
+// Colour of each pixel from its winning micropolygon: the diffuse factor the
+// fused kernel stored, the draw's colour (kernels/reyes.cl:191), and the
+// winning depth (kernels/reyes.cl:389).
 template <int PS>
-__device__ __forceinline__ float4 mp_color(const DrawDev* draws, const FrameDev& fr, const SubPatches& sub,
-                                           unsigned id) {
-    const unsigned s = id / (PS * PS), q = id % (PS * PS);
-    const int nu = (int)(q % PS), nv = (int)(q / PS);
-    const float4 r = sub.range[s];
-    const int2 m = sub.meta[s];
-    const DrawDev& d = draws[m.y];
-    const float4* P = d.cp + (size_t)m.x * (d.type == 0 ? 16 : 20);
-    float4 pos[4];
-#pragma unroll
-    for (int k = 0; k < 4; ++k) pos[k] = dice_eye(d, fr, P, r, nu + (k & 1), nv + (k >> 1));
-    return shade_quad(pos, d.color);
-}
-
-template <int PS>
-__global__ void resolve_kernel(const DrawDev* __restrict__ draws, FrameDev fr, SubPatches sub, Framebuffer fb) {
+__global__ void resolve_kernel(const DrawDev* __restrict__ draws, FrameDev fr, SubPatches sub, Framebuffer fb,
+                               const float* __restrict__ mshade) {
     long long n = fb.pixels * fb.views;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         unsigned long long key = fb.keys[i];
@@ -361,7 +385,9 @@ __global__ void resolve_kernel(const DrawDev* __restrict__ draws, FrameDev fr, S
             fb.color[i] = make_float4(fr.clear[0], fr.clear[1], fr.clear[2], fr.clear[3]);
             fb.depth[i] = 0x7fffffff;
         } else {
-            fb.color[i] = mp_color<PS>(draws, fr, sub, (unsigned)(key & 0xffffffffu));
+            const unsigned id = (unsigned)(key & 0xffffffffu);
+            const int draw = sub.meta[id / (PS * PS)].y;
+            fb.color[i] = shade_color(mshade[id], draws[draw].color);
             fb.depth[i] = (int)(key >> 32);
         }
     }
@@ -519,7 +545,10 @@ int fused_grid_impl() {
     int dev = 0, sms = 0, per_sm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, raster_fused_kernel<PS>, kRasterWarps * 32, 0);
+    cudaFuncSetAttribute(raster_fused_kernel<PS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)sizeof(FusedSmem<PS>));
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, raster_fused_kernel<PS>, kFusedThreads,
+                                                  sizeof(FusedSmem<PS>));
     if (per_sm < 1) per_sm = 1;
     return sms * per_sm;
 }
@@ -543,11 +572,14 @@ void launch_clear(const Framebuffer& fb, const FrameDev& fr, int with_color, cud
 int raster_fused_grid(int PS) { return PS == 16 ? fused_grid_impl<16>() : fused_grid_impl<8>(); }
 
 void launch_raster_fused(const DrawDev* draws, const FrameDev& fr, const SubPatches& sub, const Framebuffer& fb,
-                         BigQuad* big, long long big_cap, unsigned long long* ctrl, int grid, cudaStream_t s) {
+                         float* mshade, BigQuad* big, long long big_cap, unsigned long long* ctrl, int grid,
+                         cudaStream_t s) {
     if (fr.PS == 16)
-        raster_fused_kernel<16><<<grid, kRasterWarps * 32, 0, s>>>(draws, fr, sub, fb, big, big_cap, ctrl);
+        raster_fused_kernel<16><<<grid, kFusedThreads, sizeof(FusedSmem<16>), s>>>(draws, fr, sub, fb, mshade, big,
+                                                                                  big_cap, ctrl);
     else
-        raster_fused_kernel<8><<<grid, kRasterWarps * 32, 0, s>>>(draws, fr, sub, fb, big, big_cap, ctrl);
+        raster_fused_kernel<8><<<grid, kFusedThreads, sizeof(FusedSmem<8>), s>>>(draws, fr, sub, fb, mshade, big,
+                                                                                big_cap, ctrl);
 }
 
 void launch_raster_big(const DrawDev*, const FrameDev& fr, const Framebuffer& fb, const BigQuad* big,
@@ -556,12 +588,12 @@ void launch_raster_big(const DrawDev*, const FrameDev& fr, const Framebuffer& fb
 }
 
 void launch_resolve(const DrawDev* draws, const FrameDev& fr, const SubPatches& sub, const Framebuffer& fb,
-                    cudaStream_t s) {
+                    const float* mshade, cudaStream_t s) {
     int g = grid_for(fb.pixels * fb.views, 256);
     if (fr.PS == 16)
-        resolve_kernel<16><<<g, 256, 0, s>>>(draws, fr, sub, fb);
+        resolve_kernel<16><<<g, 256, 0, s>>>(draws, fr, sub, fb, mshade);
     else
-        resolve_kernel<8><<<g, 256, 0, s>>>(draws, fr, sub, fb);
+        resolve_kernel<8><<<g, 256, 0, s>>>(draws, fr, sub, fb, mshade);
 }
 
 void launch_dice_grid(const DrawDev* draws, const FrameDev& fr, const SubPatches& sub, long long base, int count,

@@ -141,6 +141,15 @@ class Renderer:
         self._ck(lib().mp_read_framebuffer(self._ctx, view, _f32p(color), _i32p(depth), int(linear)))
         return color, depth
 
+    def copy_framebuffer_device(self, view: int, color_ptr: int, depth_ptr: int = 0) -> None:
+        self._ck(lib().mp_copy_framebuffer_device(self._ctx, view, ctypes.c_void_p(color_ptr or None),
+                                                  ctypes.c_void_p(depth_ptr or None)))
+
+    def visibility(self, view: int = 0) -> np.ndarray:
+        ids = np.zeros(self.width * self.height, np.int64)
+        self._ck(lib().mp_read_visibility(self._ctx, view, ids.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))))
+        return ids
+
     def subpatches(self):
         cnt = ctypes.c_int64()
         self._ck(lib().mp_subpatches(self._ctx, ctypes.byref(cnt), None, None, None, 0))
@@ -175,6 +184,9 @@ class Renderer:
         self._ck(lib().mp_dice_subpatches(self._ctx, draw, n, _i32p(pid), _f32p(rng), _f32p(pos), _i32p(pxl),
                                           _f32p(dep)))
         return pos, pxl, dep
+
+    def set_displacement_amplitude(self, amp: float) -> None:
+        self._ck(lib().mp_set_displacement_amplitude(self._ctx, float(amp)))
 
     def set_grad_buffer(self, draw: int, dev_ptr: int) -> None:
         self._ck(lib().mp_set_grad_buffer(self._ctx, draw, ctypes.c_void_p(dev_ptr)))
