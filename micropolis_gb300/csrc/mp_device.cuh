@@ -146,64 +146,69 @@ struct RangeBound {
     float vlen, hlen;
 };
 
+__device__ __forceinline__ void bbox_add(RangeBound& b, const F3& p) {
+    b.bmin.x = minimum(p.x, b.bmin.x);
+    b.bmin.y = minimum(p.y, b.bmin.y);
+    b.bmin.z = minimum(p.z, b.bmin.z);
+    b.bmax.x = maximum(p.x, b.bmax.x);
+    b.bmax.y = maximum(p.y, b.bmax.y);
+    b.bmax.z = maximum(p.z, b.bmax.z);
+}
+
+// The 9 samples are visited column by column (iv outer, iu inner) so that
+// only one column and the previous one are live.  Every value is formed by
+// the reference's operations in the reference's order: the column sum v_iv is
+// (0 + d01) + d12, the row sums h_iu accumulate across columns in the same
+// order, vlen/hlen take maximum() in index order 0, 1, 2, and the bbox
+// (minimum/maximum that skip NaN) does not depend on the visiting order.
 __device__ __forceinline__ RangeBound bound_range(const DrawDev& d, int pid, float4 r) {
-    F3 ps[3][3];
     float sv[3], su[3];
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
         sv[i] = fadd(r.x, fmul(fmul(fsub(r.z, r.x), (float)i), 0.5f));
         su[i] = fadd(r.y, fmul(fmul(fsub(r.w, r.y), (float)i), 0.5f));
     }
-    if (d.type == 0) {
-        const float4* P = d.cp + (size_t)pid * 16;
-#pragma unroll
-        for (int iv = 0; iv < 3; ++iv) {
-            SplineW wt = spline_weights(su[iv]);
-            F3 row[4];
-#pragma unroll
-            for (int i = 0; i < 4; ++i)
-                row[i] = spline3(wt, ld3(P + 4 * i + 0), ld3(P + 4 * i + 1), ld3(P + 4 * i + 2),
-                                 ld3(P + 4 * i + 3));
-#pragma unroll
-            for (int iu = 0; iu < 3; ++iu)
-                ps[iu][iv] = mv_point(d.mv, spline3(spline_weights(sv[iu]), row[0], row[1], row[2], row[3]));
-        }
-    } else {
-        const float4* P = d.cp + (size_t)pid * 20;
-#pragma unroll
-        for (int iu = 0; iu < 3; ++iu)
-#pragma unroll
-            for (int iv = 0; iv < 3; ++iv) ps[iu][iv] = mv_point(d.mv, eval_gregory_cpu(P, su[iv], sv[iu]));
-    }
     RangeBound b;
     const float inf = __int_as_float(0x7f800000);
     b.bmin = F3{inf, inf, inf};
     b.bmax = F3{-inf, -inf, -inf};
-#pragma unroll
-    for (int iu = 0; iu < 3; ++iu)
-#pragma unroll
-        for (int iv = 0; iv < 3; ++iv) {
-            const F3& p = ps[iu][iv];
-            b.bmin.x = minimum(p.x, b.bmin.x);
-            b.bmin.y = minimum(p.y, b.bmin.y);
-            b.bmin.z = minimum(p.z, b.bmin.z);
-            b.bmax.x = maximum(p.x, b.bmax.x);
-            b.bmax.y = maximum(p.y, b.bmax.y);
-            b.bmax.z = maximum(p.z, b.bmax.z);
-        }
     b.vlen = 0.0f;
+    float hsum[3] = {0.0f, 0.0f, 0.0f};
+    F3 prev[3];
+#pragma unroll
+    for (int iv = 0; iv < 3; ++iv) {
+        F3 cur[3];
+        if (d.type == 0) {
+            // eval_patch(P, t = u, s = v): rows P[i][0..3] in t, then the column in s
+            const float4* P = d.cp + (size_t)pid * 16;
+            SplineW wt = spline_weights(su[iv]);
+            F3 row[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+                row[i] = spline3(wt, ld3(P + 4 * i + 0), ld3(P + 4 * i + 1), ld3(P + 4 * i + 2), ld3(P + 4 * i + 3));
+#pragma unroll
+            for (int iu = 0; iu < 3; ++iu)
+                cur[iu] = mv_point(d.mv, spline3(spline_weights(sv[iu]), row[0], row[1], row[2], row[3]));
+        } else {
+            const float4* P = d.cp + (size_t)pid * 20;
+#pragma unroll
+            for (int iu = 0; iu < 3; ++iu) cur[iu] = mv_point(d.mv, eval_gregory_cpu(P, su[iv], sv[iu]));
+        }
+#pragma unroll
+        for (int iu = 0; iu < 3; ++iu) bbox_add(b, cur[iu]);
+        // column iv: v = (0 + d(ps[0][iv], ps[1][iv])) + d(ps[1][iv], ps[2][iv])
+        float v = fadd(fadd(0.0f, distance3(cur[0], cur[1])), distance3(cur[1], cur[2]));
+        b.vlen = maximum(v, b.vlen);
+        if (iv > 0) {
+#pragma unroll
+            for (int iu = 0; iu < 3; ++iu) hsum[iu] = fadd(hsum[iu], distance3(prev[iu], cur[iu]));
+        }
+#pragma unroll
+        for (int iu = 0; iu < 3; ++iu) prev[iu] = cur[iu];
+    }
     b.hlen = 0.0f;
 #pragma unroll
-    for (int i = 0; i < 3; ++i) {
-        float h = 0.0f, v = 0.0f;
-#pragma unroll
-        for (int j = 0; j < 2; ++j) {
-            v = fadd(v, distance3(ps[j][i], ps[j + 1][i]));
-            h = fadd(h, distance3(ps[i][j], ps[i][j + 1]));
-        }
-        b.vlen = maximum(v, b.vlen);
-        b.hlen = maximum(h, b.hlen);
-    }
+    for (int iu = 0; iu < 3; ++iu) b.hlen = maximum(hsum[iu], b.hlen);
     return b;
 }
 
