@@ -175,6 +175,19 @@ mp_status mp_update_patches_device(mp_ctx* ctx, uint64_t handle, const void* dev
  * plain path; the reference's CL::PrefixSum, src/CL/PrefixSum.cpp:33-80). */
 mp_status mp_inclusive_scan(mp_ctx* ctx, const int32_t* host_in, int32_t* host_out, int64_t n);
 
+/* Inclusive prefix sum of n int32 values already in device memory, for callers
+ * that may not allocate device memory (e.g. a render loop with a fixed device
+ * budget, where cudaFree would stall the device mid-frame, or a host whose own
+ * allocator owns all device memory).  Has no counterpart in the reference.
+ * It allocates nothing: the caller passes input and output, and the scan's
+ * scratch (33 KB of look-back state) is a fixed __device__ array of the
+ * library.  n may be at most 4,194,304 (MP_ERR_INVALID_ARG beyond).  The
+ * first call on a device looks up that array's device address, so make it
+ * before any stream capture.  All calls on a device share the array: calls
+ * that overlap on the GPU race and must be serialized by the caller.  Runs on
+ * `stream` (a cudaStream_t, NULL = default stream) and returns when done. */
+mp_status mp_inclusive_scan_noalloc(const int32_t* in_dev, int32_t* out_dev, int64_t n, void* stream);
+
 /* 64-bit atomicMin throughput probe (atomics per second): pattern 0 uniform
  * random slots, pattern 1 micropolygon-like locality. */
 mp_status mp_atomic_bench(mp_ctx* ctx, int64_t n_slots, int64_t n_ops, int32_t pattern, double* atomics_per_s);
