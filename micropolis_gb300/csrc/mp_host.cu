@@ -142,8 +142,8 @@ void perspective(float fovy_rad, float aspect, float zn, float zf, float* m) {
 }
 
 // first-frame guesses; both grow (and the frame is rendered again) on overflow
-long long auto_queue_cap(long long roots) { return std::min(std::max(1LL << 22, roots * 640), 1LL << 28); }
-long long auto_sub_cap(long long roots) { return std::min(std::max(1LL << 20, roots * 320), 1LL << 26); }
+long long auto_queue_cap(long long roots) { return std::min(std::max(1LL << 22, roots * 128), 1LL << 28); }
+long long auto_sub_cap(long long roots) { return std::min(std::max(1LL << 21, roots * 64), 1LL << 26); }
 
 mp_status grow_queue(mp_ctx* c, long long need) {
     if (need <= c->q.capacity) return MP_OK;

@@ -29,6 +29,9 @@ class ReyesOptions:
     displacement_amplitude: float = 1.0        # multiplier on the hard-coded amplitudes
     batch_views: int = 1                       # framebuffer layers (batched views)
     path: str = "batched"                      # "plain" (per-pass) or "batched"
+    queue_capacity: int = 0                    # first-frame capacities (0 = automatic; they grow)
+    subpatch_capacity: int = 0
+    spin_limit: int = 0                        # bounded-wait iterations (0 = default)
 
     def update(self, **kw) -> "ReyesOptions":
         for k, v in kw.items():

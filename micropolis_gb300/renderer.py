@@ -66,6 +66,10 @@ class Renderer:
             o.clear_color[i] = opts.clear_color[i]
         o.batch_views = opts.batch_views
         o.path = _lib.MP_PATH_PLAIN if opts.path == "plain" else _lib.MP_PATH_BATCHED
+        o.queue_capacity = opts.queue_capacity
+        o.subpatch_capacity = opts.subpatch_capacity
+        if opts.spin_limit:
+            o.spin_limit = opts.spin_limit
         self._ctx = ctypes.c_void_p()
         st = lib().mp_create(ctypes.byref(o), ctypes.byref(self._ctx))
         if st != 0:

@@ -1,0 +1,154 @@
+"""Edge cases of the GPU path against the oracle, through the C ABI: empty and
+fully culled scenes, NaN control points, the depth cap, patches crossing the
+eye plane, capacity overflow and regrowth, bounded waits, 16x16 dicing,
+backface culling off, and many independent views in one batched frame."""
+import numpy as np
+import pytest
+
+from helpers import framebuffer_diff, subpatch_set
+
+pytestmark = pytest.mark.gpu
+
+REL_TOL = 1e-5
+COVERAGE_BUDGET = 1e-4
+
+
+def _render(scene, path="batched", **over):
+    from micropolis_gb300.renderer import render_scene, renderer_for
+    r = renderer_for(scene, path, **over)
+    render_scene(r, scene)
+    return r
+
+
+def _oracle(scene, **over):
+    from oracle import oracle
+    p = oracle.make_params(scene, **over)
+    s = set()
+    for k in range(len(scene.draws)):
+        pid, rng, _ = oracle.bound_n_split(scene, k, params=p)
+        s |= subpatch_set(pid, rng, np.full(len(pid), k))
+    col, dep, st = oracle.render(scene, params=p)
+    return s, col, dep, st
+
+
+def _check(scene, path="batched", **over):
+    r = _render(scene, path, **over)
+    want, ocol, odep, ost = _oracle(scene, **over)
+    d, p, g = r.subpatches()
+    assert subpatch_set(p, g, d) == want
+    col, dep = r.read_framebuffer()
+    bad, _ = framebuffer_diff(col, dep, ocol, odep, REL_TOL)
+    assert bad <= COVERAGE_BUDGET * dep.size, bad
+    assert r.stats()["fragments"] == ost["fragments"]
+    r.close()
+    return len(want)
+
+
+def _small_scene(**kw):
+    from micropolis_gb300 import scenes
+    return scenes.mixed4096_1920x1080(n=kw.pop("n", 128), width=kw.pop("width", 512), height=kw.pop("height", 512),
+                                      **kw)
+
+
+def test_empty_mesh(built, cuda):
+    from micropolis_gb300 import scenes
+    sc = _small_scene()
+    sc.draws[0].mesh = scenes.Mesh(scenes.BEZIER, np.zeros((0, 16, 3), np.float32))
+    for path in ("batched", "plain"):
+        _check(sc, path)
+
+
+def test_everything_culled(built, cuda):
+    from micropolis_gb300 import scenes
+    sc = _small_scene()
+    for d in sc.draws:   # look away from the scene
+        d.mv = scenes.look_at((0, 0, 40), (0, 0, 80), (0, 1, 0))
+    for path in ("batched", "plain"):
+        r = _render(sc, path)
+        assert r.stats()["subpatches"] == 0
+        col, dep = r.read_framebuffer()
+        assert np.all(dep == 0x7FFFFFFF)
+        r.close()
+
+
+def test_nan_control_points(built, cuda):
+    sc = _small_scene()
+    cp = sc.draws[0].mesh.cp
+    cp[3, 5, 1] = np.nan      # one interior point of one Bezier patch
+    cp[7, :, :] = np.nan      # a whole patch
+    sc.draws[1].mesh.cp[2, 13, 0] = np.nan
+    for path in ("batched", "plain"):
+        _check(sc, path)
+
+
+@pytest.mark.parametrize("depth", [0, 3])
+def test_depth_cap(built, cuda, depth):
+    sc = _small_scene()
+    _check(sc, "batched", max_split_depth=depth)
+
+
+def test_eye_plane_crossing(built, cuda):
+    """A heightfield seen from just above its surface: patches straddle z = 0
+    in eye space and hit the depth cap near the eye."""
+    from micropolis_gb300 import scenes
+    sc = scenes.heightfield_1024x768()
+    sc.width, sc.height = 512, 384
+    sc.draws[0].mv = scenes.look_at((0.0, -0.3, 0.05), (0.0, 1.0, 0.0), (0, 0, 1))
+    n = _check(sc, "batched", max_split_depth=12)
+    assert n > 0
+
+
+def test_overflow_regrowth(built, cuda):
+    """Tiny first capacities: the frame regrows its buffers and matches."""
+    sc = _small_scene(n=256)
+    _check(sc, "batched", queue_capacity=256, subpatch_capacity=16)
+
+
+def test_bounded_wait_reports_timeout(built, cuda):
+    """With a spin limit of one iteration the persistent bound-and-split gives
+    up waiting and reports MP_ERR_TIMEOUT (or finishes); it never hangs, and
+    the device stays usable."""
+    from micropolis_gb300 import _lib
+    sc = _small_scene(n=512)
+    try:
+        _render(sc, "batched", spin_limit=1).close()
+        status = 0
+    except _lib.MpError as e:
+        status = e.status
+    assert status in (_lib.MP_OK, _lib.MP_ERR_TIMEOUT)
+    _check(sc, "batched")   # a fresh context still renders correctly
+
+
+def test_dice16(built, cuda):
+    sc = _small_scene()
+    _check(sc, "batched", reyes_patch_size=16)
+    _check(sc, "plain", reyes_patch_size=16)
+
+
+def test_backface_culling_off(built, cuda):
+    sc = _small_scene()
+    _check(sc, "batched", backface_culling=False)
+
+
+def test_many_views_batched_equals_per_view_plain(built, cuda):
+    """Independent scenes in one batched frame (one layer each) equal the same
+    scenes rendered one by one with the plain path."""
+    from micropolis_gb300 import scenes
+    sc = scenes.views64_512x512(n_views=8, size=256)
+    for d in sc.draws:  # keep the test quick: at most 400 patches per view
+        d.mesh = scenes.Mesh(d.mesh.type, d.mesh.cp[:400])
+    rb = _render(sc, "batched")
+    db, pb, gb = rb.subpatches()
+    for v, d in enumerate(sc.draws):
+        one = scenes.Scene(sc.name, sc.width, sc.height, [scenes.Draw(d.mesh, d.mv, d.color, 0)],
+                           options={k: x for k, x in sc.options.items() if k != "batch_views"})
+        rp = _render(one, "plain")
+        _, pp, gp = rp.subpatches()
+        sel = db == v
+        assert subpatch_set(pb[sel], gb[sel]) == subpatch_set(pp, gp)
+        cb, zb = rb.read_framebuffer(view=v)
+        cp_, zp = rp.read_framebuffer()
+        bad, _ = framebuffer_diff(cb, zb, cp_, zp, REL_TOL)
+        assert bad <= COVERAGE_BUDGET * zb.size
+        rp.close()
+    rb.close()
