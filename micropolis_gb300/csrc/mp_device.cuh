@@ -12,7 +12,8 @@
 //     kernels/utility.h): the rounding choices allowed by the reference's
 //     -cl-mad-enable -cl-fast-relaxed-math build are fixed as
 //       R1 a*b + c is one fma; a*b + c*d = fma(c, d, a*b); a*b - c*d = fma(-c, d, a*b)
-//       R2 division and sqrt correctly rounded
+//       R2 a division x / y is x * RN(1 / y) (the reciprocal correctly rounded,
+//          as -cl-fast-relaxed-math permits); sqrt correctly rounded
 //       R3 max(x, 0) ignores NaN (fmaxf)
 //       R4 float->int truncates and saturates, NaN -> 0 (cvt.rzi.s32.f32)
 //       R5 int arithmetic wraps modulo 2^32
@@ -261,6 +262,9 @@ __device__ __forceinline__ void split_children(float4 r, int dec, float4& c0, fl
 // Kernel restatement arithmetic (R1-R6).
 
 __device__ __forceinline__ float ffma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+// R2: x / y in the kernel restatement
+__device__ __forceinline__ float frcp(float y) { return __frcp_rn(y); }
+__device__ __forceinline__ float kdiv(float x, float y) { return fmul(x, frcp(y)); }
 
 // R6: sin/cos by Cody-Waite reduction with pi/2 = P1 + P2 + P3 (three floats
 // from the exact value of pi) and Taylor polynomials (degree 9 / 10) on
@@ -325,8 +329,9 @@ __device__ __forceinline__ float4 eval_bezier_dice(const float4* P, float tx, fl
 }
 
 __device__ __forceinline__ float4 blend4(float a, float4 A, float b, float4 B, float den) {
-    return make_float4(sel_nan(fdiv(ffma(b, B.x, fmul(a, A.x)), den)), sel_nan(fdiv(ffma(b, B.y, fmul(a, A.y)), den)),
-                       sel_nan(fdiv(ffma(b, B.z, fmul(a, A.z)), den)), sel_nan(fdiv(ffma(b, B.w, fmul(a, A.w)), den)));
+    const float r = frcp(den);
+    return make_float4(sel_nan(fmul(ffma(b, B.x, fmul(a, A.x)), r)), sel_nan(fmul(ffma(b, B.y, fmul(a, A.y)), r)),
+                       sel_nan(fmul(ffma(b, B.z, fmul(a, A.z)), r)), sel_nan(fmul(ffma(b, B.w, fmul(a, A.w)), r)));
 }
 
 // kernels/utility.h:155-206 -- Gregory patch with NaN face blends zeroed.
@@ -384,7 +389,7 @@ __device__ __forceinline__ float4 displace(float4 pos, const float* fd) {
 // nu / PS is exact (PS is a power of two), so it is formed as nu * (1 / PS).
 __device__ __forceinline__ float4 dice_eye_m(int type, const float* mv, const FrameDev& fr, const float4* P,
                                              float4 r, int nu, int nv) {
-    const float inv = fr.PS == 16 ? 0.0625f : 0.125f;  // 1 / PS, PS in {8, 16}
+    const float inv = fr.PS == 16 ? 0.0625f : 0.125f;  // RN(1 / PS), exact for PS in {8, 16}
     float tx = ffma(fsub(r.z, r.x), fmul((float)nu, inv), r.x);
     float ty = ffma(fsub(r.w, r.y), fmul((float)nv, inv), r.y);
     float4 o = (type == 0) ? eval_bezier_dice(P, tx, ty) : eval_gregory_dice(P, tx, ty);
@@ -402,11 +407,12 @@ __device__ __forceinline__ void project_vertex_m(const float* proj, const FrameD
                                                  int& py, float& depth) {
     float4 p = mul_m44v4(proj, pos);
     int vsx = fr.W << fr.shift, vsy = fr.H << fr.shift;
-    float ex = fadd(fmul(fmul(fdiv(p.x, p.w), (float)vsx), 0.5f), (float)(vsx / 2));
-    float ey = fadd(fmul(fmul(fdiv(p.y, p.w), (float)vsy), 0.5f), (float)(vsy / 2));
+    const float rw = frcp(p.w);
+    float ex = fadd(fmul(fmul(fmul(p.x, rw), (float)vsx), 0.5f), (float)(vsx / 2));
+    float ey = fadd(fmul(fmul(fmul(p.y, rw), (float)vsy), 0.5f), (float)(vsy / 2));
     px = __float2int_rz(ex);
     py = __float2int_rz(ey);
-    depth = fdiv(p.z, p.w);
+    depth = fmul(p.z, rw);
 }
 __device__ __forceinline__ void project_vertex(const DrawDev& d, const FrameDev& fr, float4 pos, int& px, int& py,
                                                float& depth) {
@@ -419,8 +425,8 @@ __device__ __forceinline__ V3 cross3(V3 a, V3 b) {
     return V3{ffma(-a.z, b.y, fmul(a.y, b.z)), ffma(-a.x, b.z, fmul(a.z, b.x)), ffma(-a.y, b.x, fmul(a.x, b.y))};
 }
 __device__ __forceinline__ V3 normalize3(V3 v) {
-    float l = __fsqrt_rn(dot3(v, v));
-    return V3{fdiv(v.x, l), fdiv(v.y, l), fdiv(v.z, l)};
+    const float r = frcp(__fsqrt_rn(dot3(v, v)));
+    return V3{fmul(v.x, r), fmul(v.y, r), fmul(v.z, r)};
 }
 
 // kernels/reyes.cl:172-191 -- flat shading of a quad from its 4 eye positions
@@ -497,7 +503,7 @@ __device__ __forceinline__ bool tri_test(const Tri& t, int tx, int ty, float& de
         for (int e = 0; e < 3; ++e) {
             int en = (e + 1) % 3;
             int dn = wsub(wadd(wmul(t.Dx[en], t.Px[e]), wmul(t.Dy[en], t.Py[e])), t.O[en]);
-            w[e] = fdiv((float)V[en], (float)dn);
+            w[e] = kdiv((float)V[en], (float)dn);
         }
         float d = ffma(t.dv[2], w[2], ffma(t.dv[1], w[1], fmul(t.dv[0], w[0])));
         if (d < depth) depth = d;
@@ -507,7 +513,7 @@ __device__ __forceinline__ bool tri_test(const Tri& t, int tx, int ty, float& de
 
 // idepth = (int)(clamp(depth / 200, 0, 1) * 0x7fffffff) (kernels/reyes.cl:364)
 __device__ __forceinline__ unsigned idepth_of(float depth) {
-    float c = fminf(fmaxf(fdiv(depth, 200.0f), 0.0f), 1.0f);
+    float c = fminf(fmaxf(kdiv(depth, 200.0f), 0.0f), 1.0f);
     return (unsigned)__float2int_rz(fmul(c, 2147483648.0f));
 }
 

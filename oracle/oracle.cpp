@@ -12,7 +12,8 @@
 //   R1  an expression a*b + c (or c + a*b) is one fused multiply-add;
 //       a*b + c*d is fma(c, d, a*b) (right product fused);
 //       a*b - c*d is fma(-c, d, a*b);
-//   R2  division and square root are correctly rounded (IEEE);
+//   R2  a division x / y is x * RN(1 / y), the reciprocal correctly rounded
+//       (-cl-fast-relaxed-math permits it); square root is correctly rounded;
 //   R3  max(x, 0) on floats ignores a NaN operand (fmaxf);
 //   R4  float -> int conversion truncates, saturates at the int range and
 //       maps NaN to 0 (the CUDA cvt.rzi.s32.f32 rule);
@@ -266,6 +267,9 @@ static inline int32_t f2i_rz_sat(float x) {
 
 static inline float fmaxnan(float a, float b) { return std::fmax(a, b); }
 
+// R2
+static inline float kdiv(float x, float y) { return x * (1.0f / y); }
+
 }  // namespace
 
 // R6: sin/cos by Cody-Waite reduction with pi/2 = P1 + P2 + P3 (three floats
@@ -352,10 +356,10 @@ static inline V4 eval_gregory_k(const float* cp, float tx, float ty) {
     auto blend = [&](float a, V4 A, float b, V4 B, float den) {
         // (a*A + b*B) / den with R1: fma(b, B, a*A)
         V4 r;
-        r.x = sel_nan(std::fma(b, B.x, a * A.x) / den);
-        r.y = sel_nan(std::fma(b, B.y, a * A.y) / den);
-        r.z = sel_nan(std::fma(b, B.z, a * A.z) / den);
-        r.w = sel_nan(std::fma(b, B.w, a * A.w) / den);
+        r.x = sel_nan(kdiv(std::fma(b, B.x, a * A.x), den));
+        r.y = sel_nan(kdiv(std::fma(b, B.y, a * A.y), den));
+        r.z = sel_nan(kdiv(std::fma(b, B.z, a * A.z), den));
+        r.w = sel_nan(kdiv(std::fma(b, B.w, a * A.w), den));
         return r;
     };
     V4 F0 = blend(u, P(12), v, P(16), u + v);
@@ -403,7 +407,7 @@ static inline V3 cross3(const V3& a, const V3& b) {
 
 static inline V3 normalize3(const V3& v) {
     float l = std::sqrt(dot3(v, v));
-    return V3{v.x / l, v.y / l, v.z / l};
+    return V3{kdiv(v.x, l), kdiv(v.y, l), kdiv(v.z, l)};
 }
 
 // glm::perspective<float>(fovy, aspect, near, far), right-handed, depth -1..1.
@@ -485,11 +489,11 @@ struct Frame {
         }
         V4 p = mul_m44v4(proj, pos);
         int32_t vsx = W << shift, vsy = H << shift;
-        float ex = (p.x / p.w * (float)vsx) / 2 + (float)(vsx / 2);
-        float ey = (p.y / p.w * (float)vsy) / 2 + (float)(vsy / 2);
+        float ex = (kdiv(p.x, p.w) * (float)vsx) / 2 + (float)(vsx / 2);
+        float ey = (kdiv(p.y, p.w) * (float)vsy) / 2 + (float)(vsy / 2);
         px = f2i_rz_sat(ex);
         py = f2i_rz_sat(ey);
-        dep = p.z / p.w;
+        dep = kdiv(p.z, p.w);
     }
 
     // kernels/reyes.cl:172-191 -- flat colour of a quad from its 4 eye positions
@@ -530,7 +534,7 @@ struct Frame {
         for (int e = 0; e < 3; ++e) {
             int en = (e + 1) % 3;
             Dn[e] = wsub(wadd(wmul(Dx[en], Px[e]), wmul(Dy[en], Py[e])), O[en]);
-            w[e] = (float)V[en] / (float)Dn[e];
+            w[e] = kdiv((float)V[en], (float)Dn[e]);
         }
         float d = std::fma(dv[2], w[2], std::fma(dv[1], w[1], dv[0] * w[0]));
         *depth = (success && d < *depth) ? d : *depth;
@@ -637,7 +641,7 @@ struct Frame {
                                         int in2 = inside_triangle(t2x, t2y, tpx, tpy, d2, &depth);
                                         if (!(in1 || in2)) continue;
                                         ++n_frag;
-                                        float cl = std::min(std::max(depth / 200.0f, 0.0f), 1.0f);
+                                        float cl = std::min(std::max(kdiv(depth, 200.0f), 0.0f), 1.0f);
                                         int32_t idepth = f2i_rz_sat(cl * (float)0x7fffffff);
                                         int64_t fb = fb_pos(tx * 8 + x, ty * 8 + y);
                                         if (idepth < this->depth[fb]) {
