@@ -307,25 +307,43 @@ __device__ __forceinline__ float mp_cosf(float x) {
 __device__ __forceinline__ float sel_nan(float x) { return isnan(x) ? 0.0f : x; }
 
 // kernels/utility.h:121-152 -- p += (v_i * c_j) * P[4i + j], i-major; P.w = 1.
-__device__ __forceinline__ float4 eval_bezier_dice(const float4* P, float tx, float ty) {
-    float sx = fsub(1.0f, tx), sy = fsub(1.0f, ty);
-    float vw[4] = {fmul(fmul(sx, sx), sx), fmul(fmul(fmul(3.0f, sx), sx), tx), fmul(fmul(fmul(3.0f, sx), tx), tx),
-                   fmul(fmul(tx, tx), tx)};
-    float cw[4] = {fmul(fmul(sy, sy), sy), fmul(fmul(fmul(3.0f, ty), sy), sy), fmul(fmul(fmul(3.0f, ty), ty), sy),
-                   fmul(fmul(ty, ty), ty)};
+// Row weights v_i (in t.x) and column weights c_j (in t.y) of
+// kernels/utility.h:127-145: v = s^3, 3 s^2 t, 3 s t^2, t^3 with the
+// source's left-to-right products.
+__device__ __forceinline__ float4 row_weights(float tx) {
+    float sx = fsub(1.0f, tx);
+    return make_float4(fmul(fmul(sx, sx), sx), fmul(fmul(fmul(3.0f, sx), sx), tx), fmul(fmul(fmul(3.0f, sx), tx), tx),
+                       fmul(fmul(tx, tx), tx));
+}
+__device__ __forceinline__ float4 col_weights(float ty) {
+    float sy = fsub(1.0f, ty);
+    return make_float4(fmul(fmul(sy, sy), sy), fmul(fmul(fmul(3.0f, ty), sy), sy), fmul(fmul(fmul(3.0f, ty), ty), sy),
+                       fmul(fmul(ty, ty), ty));
+}
+// p += (v_i * c_j) * Q_{4i+j}, i-major, one fma per component (R1).
+template <typename Pts>
+__device__ __forceinline__ float4 accumulate16(const Pts& Q, float4 vw4, float4 cw4) {
+    const float vw[4] = {vw4.x, vw4.y, vw4.z, vw4.w};
+    const float cw[4] = {cw4.x, cw4.y, cw4.z, cw4.w};
     float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
     for (int i = 0; i < 4; ++i)
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
             float w = fmul(vw[i], cw[j]);
-            float4 c = P[4 * i + j];
+            float4 c = Q[4 * i + j];
             p.x = ffma(w, c.x, p.x);
             p.y = ffma(w, c.y, p.y);
             p.z = ffma(w, c.z, p.z);
             p.w = ffma(w, c.w, p.w);
         }
     return p;
+}
+__device__ __forceinline__ float4 eval_bezier_dice_w(const float4* P, float4 vw, float4 cw) {
+    return accumulate16(P, vw, cw);
+}
+__device__ __forceinline__ float4 eval_bezier_dice(const float4* P, float tx, float ty) {
+    return eval_bezier_dice_w(P, row_weights(tx), col_weights(ty));
 }
 
 __device__ __forceinline__ float4 blend4(float a, float4 A, float b, float4 B, float den) {
@@ -335,31 +353,17 @@ __device__ __forceinline__ float4 blend4(float a, float4 A, float b, float4 B, f
 }
 
 // kernels/utility.h:155-206 -- Gregory patch with NaN face blends zeroed.
-__device__ __forceinline__ float4 eval_gregory_dice(const float4* P, float tx, float ty) {
-    float sx = fsub(1.0f, tx), sy = fsub(1.0f, ty);
+__device__ __forceinline__ float4 eval_gregory_dice_w(const float4* P, float tx, float ty, float4 vw, float4 cw) {
     float u = tx, v = ty;
     float4 F0 = blend4(u, P[12], v, P[16], fadd(u, v));
     float4 F1 = blend4(fsub(1.0f, u), P[17], v, P[13], fadd(fsub(1.0f, u), v));
     float4 F2 = blend4(fsub(1.0f, u), P[14], fsub(1.0f, v), P[18], fsub(fsub(2.0f, u), v));
     float4 F3 = blend4(u, P[19], fsub(1.0f, v), P[15], fsub(fadd(1.0f, u), v));
-    float4 pts[16] = {P[0], P[4], P[9], P[1], P[8], F0, F1, P[5], P[7], F3, F2, P[10], P[3], P[11], P[6], P[2]};
-    float vw[4] = {fmul(fmul(sx, sx), sx), fmul(fmul(fmul(3.0f, sx), sx), tx), fmul(fmul(fmul(3.0f, sx), tx), tx),
-                   fmul(fmul(tx, tx), tx)};
-    float cw[4] = {fmul(fmul(sy, sy), sy), fmul(fmul(fmul(3.0f, ty), sy), sy), fmul(fmul(fmul(3.0f, ty), ty), sy),
-                   fmul(fmul(ty, ty), ty)};
-    float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
-#pragma unroll
-    for (int i = 0; i < 4; ++i)
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            float w = fmul(vw[i], cw[j]);
-            float4 c = pts[4 * i + j];
-            p.x = ffma(w, c.x, p.x);
-            p.y = ffma(w, c.y, p.y);
-            p.z = ffma(w, c.z, p.z);
-            p.w = ffma(w, c.w, p.w);
-        }
-    return p;
+    const float4 pts[16] = {P[0], P[4], P[9], P[1], P[8], F0, F1, P[5], P[7], F3, F2, P[10], P[3], P[11], P[6], P[2]};
+    return accumulate16(pts, vw, cw);
+}
+__device__ __forceinline__ float4 eval_gregory_dice(const float4* P, float tx, float ty) {
+    return eval_gregory_dice_w(P, tx, ty, row_weights(tx), col_weights(ty));
 }
 
 // dot products: a chain of fused multiply-adds from x to w (R1)
@@ -387,15 +391,23 @@ __device__ __forceinline__ float4 displace(float4 pos, const float* fd) {
 
 // Eye-space position of dice vertex (nu, nv) of a sub-patch (kernels/dice.cl:44-67).
 // nu / PS is exact (PS is a power of two), so it is formed as nu * (1 / PS).
-__device__ __forceinline__ float4 dice_eye_m(int type, const float* mv, const FrameDev& fr, const float4* P,
-                                             float4 r, int nu, int nv) {
+// Parameter of dice vertex index n along one side: mix(rmin, rmax, n / PS).
+__device__ __forceinline__ float dice_param(float rmin, float rmax, int n, const FrameDev& fr) {
     const float inv = fr.PS == 16 ? 0.0625f : 0.125f;  // RN(1 / PS), exact for PS in {8, 16}
-    float tx = ffma(fsub(r.z, r.x), fmul((float)nu, inv), r.x);
-    float ty = ffma(fsub(r.w, r.y), fmul((float)nv, inv), r.y);
-    float4 o = (type == 0) ? eval_bezier_dice(P, tx, ty) : eval_gregory_dice(P, tx, ty);
+    return ffma(fsub(rmax, rmin), fmul((float)n, inv), rmin);
+}
+// Eye position from precomputed parameters and weights of one vertex.
+__device__ __forceinline__ float4 dice_eye_w(int type, const float* mv, const FrameDev& fr, const float4* P, float tx,
+                                             float ty, float4 vw, float4 cw) {
+    float4 o = (type == 0) ? eval_bezier_dice_w(P, vw, cw) : eval_gregory_dice_w(P, tx, ty, vw, cw);
     float4 pos = mul_m44v4(mv, o);
     if (fr.displacement) pos = displace(pos, fr.fdisp);
     return pos;
+}
+__device__ __forceinline__ float4 dice_eye_m(int type, const float* mv, const FrameDev& fr, const float4* P,
+                                             float4 r, int nu, int nv) {
+    const float tx = dice_param(r.x, r.z, nu, fr), ty = dice_param(r.y, r.w, nv, fr);
+    return dice_eye_w(type, mv, fr, P, tx, ty, row_weights(tx), col_weights(ty));
 }
 __device__ __forceinline__ float4 dice_eye(const DrawDev& d, const FrameDev& fr, const float4* P, float4 r,
                                            int nu, int nv) {

@@ -157,7 +157,10 @@ struct FusedSmem {
     int2 meta[NS];
     int type[NS], view[NS];
     int bound[NS][NB][4];
+    int tiles[NS][NB][4];     // block tile range; tiles[k][b][0] > tiles[k][b][2] marks a skipped block
     unsigned zero[NS];
+    float tx[NS][G], ty[NS][G];
+    float4 vw[NS][G], cw[NS][G];
     int px[NS * NV], py[NS * NV];
     float dep[NS * NV];
     float ex[NS * NV], ey[NS * NV], ez[NS * NV];
@@ -201,12 +204,27 @@ __global__ void __launch_bounds__(kFusedThreads, FusedCfg<PS>::MINB)
             if (c < 16) sm.mv[k][c] = d.mv[c]; else sm.proj[k][c - 16] = d.proj[c - 16];
             if (c == 0) { sm.type[k] = d.type; sm.view[k] = d.view; }
         }
+        // dice parameters and Bernstein weights of each row / column of vertices
+        for (int i = tid; i < n * 2 * G; i += kFusedThreads) {
+            const int k = i / (2 * G), c = i % (2 * G);
+            const float4 rg = sm.range[k];
+            if (c < G) {
+                const float t = dice_param(rg.x, rg.z, c, fr);
+                sm.tx[k][c] = t;
+                sm.vw[k][c] = row_weights(t);
+            } else {
+                const float t = dice_param(rg.y, rg.w, c - G, fr);
+                sm.ty[k][c - G] = t;
+                sm.cw[k][c - G] = col_weights(t);
+            }
+        }
         __syncthreads();
         // dice vertices (kernels/dice.cl:37-80)
         for (int i = tid; i < n * NV; i += kFusedThreads) {
             const int k = i / NV, v = i % NV;
             const int nu = v % G, nv = v / G;
-            float4 pos = dice_eye_m(sm.type[k], sm.mv[k], fr, sm.cp[k], sm.range[k], nu, nv);
+            float4 pos = dice_eye_w(sm.type[k], sm.mv[k], fr, sm.cp[k], sm.tx[k][nu], sm.ty[k][nv], sm.vw[k][nu],
+                                    sm.cw[k][nv]);
             int px, py;
             float dep;
             project_vertex_m(sm.proj[k], fr, pos, px, py, dep);
@@ -247,13 +265,24 @@ __global__ void __launch_bounds__(kFusedThreads, FusedCfg<PS>::MINB)
             }
         }
         __syncthreads();
+        // the tile range of each block, or a skip mark
+        for (int i = tid; i < n * NB; i += kFusedThreads) {
+            const int k = i / NB, b = i % NB;
+            const int* bb = sm.bound[k][b];
+            int* t = sm.tiles[k][b];
+            if (!block_tiles(fr, bb[0], bb[1], bb[2], bb[3], !((sm.zero[k] >> b) & 1), t)) {
+                t[0] = 1;
+                t[2] = 0;
+            }
+        }
+        __syncthreads();
         // rasterize every quad of a live block
         for (int i = tid; i < n * NQ; i += kFusedThreads) {
             const int k = i / NQ, q = i % NQ;
             const int nu = q % PS, nv = q / PS, blk = (nu >> 3) + (nv >> 3) * BPL;
-            const int* bb = sm.bound[k][blk];
-            int tiles[4];
-            if (!block_tiles(fr, bb[0], bb[1], bb[2], bb[3], !((sm.zero[k] >> blk) & 1), tiles)) continue;
+            const int* tp = sm.tiles[k][blk];
+            if (tp[0] > tp[2]) continue;
+            const int tiles[4] = {tp[0], tp[1], tp[2], tp[3]};
             const int i0 = k * NV + nu + nv * G;
             const int idx[4] = {i0, i0 + 1, i0 + G, i0 + G + 1};
             int qx[4], qy[4];
