@@ -64,6 +64,11 @@ typedef struct {
     int64_t queue_capacity;         /* bound&split work items */
     int64_t subpatch_capacity;      /* emitted sub-patches per frame */
     int64_t spin_limit;             /* bounded-wait iterations before MP_ERR_TIMEOUT */
+    /* batched path: run bound&split and rasterization in one launch that
+     * rasterizes sub-patches while they are being emitted (1) or as two
+     * launches (0); bns_blocks = blocks that start with bound&split (0 = auto) */
+    int32_t overlap;
+    int32_t bns_blocks;
 } mp_options;
 
 /* The reference's Projection(fovy, near, viewport) (src/base/Projection.h:144). */

@@ -18,45 +18,11 @@
 //
 // The bound criterion of both paths is the reference's CPU one
 // (src/Reyes/BoundNSplitCLCPU.cpp:117-148), evaluated by mp::bns_decide.
-#include "mp_internal.h"
+#include "mp_bns_loop.cuh"
 
 namespace mp {
 
 namespace {
-
-__device__ __forceinline__ unsigned long long* cw(unsigned long long* ctrl, int w) { return ctrl + w * kCtrlStride; }
-
-__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
-    unsigned v;
-    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-    return v;
-}
-__device__ __forceinline__ void st_release_u32(unsigned* p, unsigned v) {
-    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
-__device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long* p) {
-    unsigned long long v;
-    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
-    return v;
-}
-__device__ __forceinline__ void st_release_u64(unsigned long long* p, unsigned long long v) {
-    asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
-}
-__device__ __forceinline__ unsigned lanemask_lt() {
-    unsigned m;
-    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
-    return m;
-}
-
-__device__ void set_status(unsigned long long* ctrl, int code) {
-    atomicCAS(cw(ctrl, kStatus), 0ull, (unsigned long long)code);
-}
-
-// kQTail packs two counters updated by one atomic: the high 32 bits count
-// queue tickets ever filled (roots included), the low 32 bits the items pushed
-// but not yet finished.  A warp step adds (2*splits << 32) + (2*splits -
-// processed); the borrow of a negative low part is cancelled by the carry.
-constexpr unsigned long long kLow32 = 0xffffffffull;
 
 __global__ void bns_reset_kernel(unsigned long long* ctrl, long long roots) {
     *cw(ctrl, kQTail) = ((unsigned long long)roots << 32) | (unsigned long long)roots;
@@ -70,11 +36,11 @@ __global__ void bns_reset_kernel(unsigned long long* ctrl, long long roots) {
     *cw(ctrl, kBigCount) = 0;
     *cw(ctrl, kFragments) = 0;
     *cw(ctrl, kBigOverflow) = 0;
+    *cw(ctrl, kGroupTicket) = 0;
 }
 
 constexpr int kBnsBlock = 128;
 constexpr int kBnsSmemDraws = 64;
-constexpr unsigned long long kNoTicket = ~0ull;
 
 __global__ void __launch_bounds__(kBnsBlock) bns_persistent_kernel(const DrawDev* __restrict__ gdraws,
                                                                    const int* __restrict__ root_prefix,
@@ -90,133 +56,7 @@ __global__ void __launch_bounds__(kBnsBlock) bns_persistent_kernel(const DrawDev
             reinterpret_cast<int*>(s_draws)[i] = __ldg(reinterpret_cast<const int*>(gdraws) + i);
         __syncthreads();
     }
-    const DrawDev* draws = staged ? s_draws : gdraws;
-    const int lane = threadIdx.x & 31;
-    const unsigned epoch = (unsigned)*(volatile unsigned long long*)cw(ctrl, kEpoch);
-    const unsigned long long R = *(volatile unsigned long long*)cw(ctrl, kRoots);
-    unsigned long long ticket = kNoTicket;
-    long long idle = 0;
-    unsigned sleep_ns = 32;
-    while (true) {
-        // hand new tickets to the lanes that have none
-        unsigned need = __ballot_sync(0xffffffffu, ticket == kNoTicket);
-        if (need) {
-            int leader = __ffs(need) - 1;
-            unsigned long long base = 0;
-            if (lane == leader) base = atomicAdd(cw(ctrl, kQHead), (unsigned long long)__popc(need));
-            base = __shfl_sync(0xffffffffu, base, leader);
-            if (ticket == kNoTicket) ticket = base + __popc(need & lanemask_lt());
-        }
-        bool ready = false;
-        if (ticket < R) {
-            ready = true;
-        } else {
-            unsigned long long slot = ticket - R;
-            if ((long long)slot < q.capacity) ready = ld_acquire_u32(q.seq + slot) == epoch;
-        }
-        unsigned rmask = __ballot_sync(0xffffffffu, ready);
-        if (rmask == 0) {
-            unsigned long long done = 0;
-            if (lane == 0) done = *(volatile unsigned long long*)cw(ctrl, kDone);
-            done = __shfl_sync(0xffffffffu, done, 0);
-            if (done) break;
-            if (++idle > spin_limit) {
-                if (lane == 0) {
-                    set_status(ctrl, kErrTimeout);
-                    st_release_u64(cw(ctrl, kDone), 1ull);
-                }
-                break;
-            }
-            __nanosleep(sleep_ns);
-            if (sleep_ns < 2048) sleep_ns <<= 1;
-            continue;
-        }
-        idle = 0;
-        sleep_ns = 32;
-
-        float4 r = make_float4(0.f, 0.f, 1.f, 1.f);
-        int pid = 0, draw = 0, depth = 0;
-        int dec = -1;
-        if (ready) {
-            if (ticket < R) {
-                // root: find the draw whose patch range holds this ticket
-                int lo = 0, hi = n_draws - 1;
-                while (lo < hi) {
-                    int mid = (lo + hi + 1) >> 1;
-                    if ((unsigned long long)__ldg(root_prefix + mid) <= ticket) lo = mid; else hi = mid - 1;
-                }
-                draw = lo;
-                pid = (int)(ticket - (unsigned long long)__ldg(root_prefix + lo));
-            } else {
-                unsigned long long slot = ticket - R;
-                r = __ldcg(q.range + slot);
-                uint2 m = __ldcg(q.meta + slot);
-                pid = (int)m.x;
-                draw = (int)(m.y & 0xffffffu);
-                depth = (int)(m.y >> 24);
-            }
-            dec = bns_decide(draws[draw], fr, pid, r, depth);
-        }
-        // emitted sub-patches
-        unsigned emask = __ballot_sync(0xffffffffu, dec == kDraw);
-        if (emask) {
-            int leader = __ffs(emask) - 1;
-            unsigned long long base = 0;
-            if (lane == leader) base = atomicAdd(cw(ctrl, kOutCount), (unsigned long long)__popc(emask));
-            base = __shfl_sync(0xffffffffu, base, leader);
-            if (dec == kDraw) {
-                unsigned long long o = base + __popc(emask & lanemask_lt());
-                if ((long long)o < out.capacity) {
-                    out.range[o] = r;
-                    out.meta[o] = make_int2(pid, draw);
-                } else {
-                    set_status(ctrl, kErrOverflow);
-                }
-            }
-        }
-        // split children: reserve their tickets and account this step's work
-        // with one packed atomic (see kQTail above)
-        const bool split = dec == kSplitX || dec == kSplitY;
-        const unsigned smask = __ballot_sync(0xffffffffu, split);
-        const long long n_child = 2ll * __popc(smask);
-        const long long net = n_child - (long long)__popc(rmask);
-        unsigned long long old = 0;
-        if (lane == 0)
-            old = atomicAdd(cw(ctrl, kQTail), ((unsigned long long)n_child << 32) + (unsigned long long)net);
-        old = __shfl_sync(0xffffffffu, old, 0);
-        bool fits = true;
-        if (split) {
-            const unsigned long long t0 = (old >> 32) + 2ull * __popc(smask & lanemask_lt());
-            const unsigned long long s0 = t0 - R;
-            fits = (long long)(s0 + 1) < q.capacity;
-            if (fits) {
-                float4 c0, c1;
-                split_children(r, dec, c0, c1);
-                const unsigned meta_y = (unsigned)draw | ((unsigned)(depth + 1) << 24);
-                q.range[s0] = c0;
-                q.range[s0 + 1] = c1;
-                q.meta[s0] = make_uint2((unsigned)pid, meta_y);
-                q.meta[s0 + 1] = make_uint2((unsigned)pid, meta_y);
-                // release: the item stores above are visible before the slot's epoch
-                st_release_u32(q.seq + s0, epoch);
-                st_release_u32(q.seq + s0 + 1, epoch);
-            } else {
-                set_status(ctrl, kErrOverflow);
-            }
-        }
-        const unsigned lost = __ballot_sync(0xffffffffu, !fits);
-        if (lane == 0) {
-            long long remaining = (long long)(old & kLow32) + net;
-            if (lost) {
-                // children that found no slot are never processed: take them back
-                const long long back = -2ll * __popc(lost);
-                unsigned long long o2 = atomicAdd(cw(ctrl, kQTail), (unsigned long long)back);
-                remaining = (long long)(o2 & kLow32) + back;
-            }
-            if (remaining == 0) st_release_u64(cw(ctrl, kDone), 1ull);
-        }
-        if (ready) ticket = kNoTicket;
-    }
+    bns_warp_loop(staged ? s_draws : gdraws, root_prefix, n_draws, fr, q, out, nullptr, ctrl, spin_limit);
 }
 
 // ---------------------------------------------------------------------------

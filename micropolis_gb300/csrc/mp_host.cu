@@ -88,7 +88,7 @@ struct mp_ctx {
     long long graph_roots = -1;
     const void* graph_key[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
 
-    int bns_grid = 0, raster_grid = 0;
+    int bns_grid = 0, raster_grid = 0, frame_grid = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     bool stage_timing = false;
     void* staging = nullptr;          // pinned upload buffer
@@ -168,6 +168,8 @@ mp_status grow_sub(mp_ctx* c, long long need, bool keep) {
     SubPatches n{};
     CK(dalloc(&n.range, cap));
     CK(dalloc(&n.meta, cap));
+    CK(dalloc(&n.seq, cap));
+    CK(cudaMemsetAsync(n.seq, 0, sizeof(unsigned) * (size_t)cap, c->stream));
     n.capacity = cap;
     if (keep && c->sub.capacity > 0) {
         CK(cudaMemcpyAsync(n.range, c->sub.range, sizeof(float4) * (size_t)c->sub.capacity, cudaMemcpyDeviceToDevice,
@@ -178,6 +180,7 @@ mp_status grow_sub(mp_ctx* c, long long need, bool keep) {
     }
     cudaFree(c->sub.range);
     cudaFree(c->sub.meta);
+    cudaFree(c->sub.seq);
     c->sub = n;
     return MP_OK;
 }
@@ -369,6 +372,24 @@ mp_status plain_draw(mp_ctx* c, int draw_index) {
 // ---------------------------------------------------------------------------
 // batched path: the whole frame as one graph
 
+int bns_blocks(const mp_ctx* c) {
+    if (c->opt.bns_blocks > 0) return std::min(c->opt.bns_blocks, c->frame_grid);
+    return std::max(1, c->frame_grid / 3);
+}
+
+// bound-and-split and rasterization: one overlapped launch or two launches
+void launch_middle(mp_ctx* c, int n) {
+    if (c->opt.overlap) {
+        launch_frame_kernel(c->d_draws, c->d_root_prefix, n, c->fr, c->q, c->sub, c->fb, c->mshade, c->big, c->big_cap,
+                            c->ctrl, c->opt.spin_limit, c->frame_grid, bns_blocks(c), c->stream);
+    } else {
+        launch_bns_persistent(c->d_draws, c->d_root_prefix, n, c->fr, c->q, c->sub, c->ctrl, c->bns_grid,
+                              c->opt.spin_limit, c->stream);
+        launch_raster_fused(c->d_draws, c->fr, c->sub, c->fb, c->mshade, c->big, c->big_cap, c->ctrl, c->raster_grid,
+                            c->stream);
+    }
+}
+
 mp_status capture_frame(mp_ctx* c, int n, long long roots) {
     invalidate_graph(c);
     cudaGraph_t g = nullptr;
@@ -378,10 +399,7 @@ mp_status capture_frame(mp_ctx* c, int n, long long roots) {
                     c->stream);
     launch_bns_reset(c->ctrl, roots, c->stream);
     launch_clear(c->fb, c->fr, 0, c->stream);
-    launch_bns_persistent(c->d_draws, c->d_root_prefix, n, c->fr, c->q, c->sub, c->ctrl, c->bns_grid,
-                          c->opt.spin_limit, c->stream);
-    launch_raster_fused(c->d_draws, c->fr, c->sub, c->fb, c->mshade, c->big, c->big_cap, c->ctrl, c->raster_grid,
-                        c->stream);
+    launch_middle(c, n);
     launch_raster_big(c->d_draws, c->fr, c->fb, c->big, c->big_cap, c->ctrl, c->stream);
     launch_resolve(c->d_draws, c->fr, c->sub, c->fb, c->mshade, c->stream);
     cudaMemcpyAsync(c->h_ctrl, c->ctrl, sizeof(unsigned long long) * kNumCtrl * kCtrlStride, cudaMemcpyDeviceToHost,
@@ -429,11 +447,17 @@ mp_status batched_frame(mp_ctx* c) {
             launch_bns_reset(c->ctrl, roots, c->stream);
             launch_clear(c->fb, c->fr, 0, c->stream);
             CK(cudaEventRecord(c->sev[0], c->stream));
-            launch_bns_persistent(c->d_draws, c->d_root_prefix, n, c->fr, c->q, c->sub, c->ctrl, c->bns_grid,
-                                  c->opt.spin_limit, c->stream);
-            CK(cudaEventRecord(c->sev[1], c->stream));
-            launch_raster_fused(c->d_draws, c->fr, c->sub, c->fb, c->mshade, c->big, c->big_cap, c->ctrl,
-                                c->raster_grid, c->stream);
+            if (c->opt.overlap) {
+                // one launch: reported under dice+raster, bound&split shows 0
+                CK(cudaEventRecord(c->sev[1], c->stream));
+                launch_middle(c, n);
+            } else {
+                launch_bns_persistent(c->d_draws, c->d_root_prefix, n, c->fr, c->q, c->sub, c->ctrl, c->bns_grid,
+                                      c->opt.spin_limit, c->stream);
+                CK(cudaEventRecord(c->sev[1], c->stream));
+                launch_raster_fused(c->d_draws, c->fr, c->sub, c->fb, c->mshade, c->big, c->big_cap, c->ctrl,
+                                    c->raster_grid, c->stream);
+            }
             CK(cudaEventRecord(c->sev[2], c->stream));
             launch_raster_big(c->d_draws, c->fr, c->fb, c->big, c->big_cap, c->ctrl, c->stream);
             CK(cudaEventRecord(c->sev[3], c->stream));
@@ -619,6 +643,7 @@ mp_status mp_create(const mp_options* opts, mp_ctx** out) {
     if (st == MP_OK) {
         c->bns_grid = bns_persistent_grid();
         c->raster_grid = raster_fused_grid(fr.PS);
+        c->frame_grid = frame_kernel_grid(fr.PS);
         launch_clear(c->fb, c->fr, 1, c->stream);
         ck(cudaStreamSynchronize(c->stream), "init");
     }
@@ -643,7 +668,7 @@ void mp_destroy(mp_ctx* c) {
     if (c->h_draws) cudaFreeHost(c->h_draws);
     if (c->h_root_prefix) cudaFreeHost(c->h_root_prefix);
     dfree(c->q.range); dfree(c->q.meta); dfree(c->q.seq);
-    dfree(c->sub.range); dfree(c->sub.meta);
+    dfree(c->sub.range); dfree(c->sub.meta); dfree(c->sub.seq);
     dfree(c->big);
     dfree(c->mshade);
     dfree(c->fb.keys); dfree(c->fb.color); dfree(c->fb.depth);

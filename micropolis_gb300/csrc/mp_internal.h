@@ -26,6 +26,7 @@ enum CtrlWord {
     kScanTotal,        // packed totals of the last scan (draws | splits << 32)
     kBigOverflow,      // big quads that did not fit
     kBigTotal,         // big quads rasterized over the frame
+    kGroupTicket,      // sub-patch groups claimed by the frame kernel's rasterizers
     kNumCtrl
 };
 constexpr int kCtrlStride = 16;  // unsigned long long words per line
@@ -41,6 +42,7 @@ struct SubPatches {         // emitted sub-patch list
     float4* range;
     int2* meta;             // (patch id, draw)
     long long capacity;
+    unsigned* seq;          // epoch of the frame that emitted the slot (frame kernel only)
 };
 
 struct BigQuad {            // a quad rasterized by the exact tile emulation
@@ -84,6 +86,13 @@ void launch_raster_fused(const DrawDev* draws, const FrameDev& fr, const SubPatc
                          float* mshade, BigQuad* big, long long big_cap, unsigned long long* ctrl, int grid,
                          cudaStream_t s);
 int raster_fused_grid(int PS);
+// bound-and-split and rasterization overlapped in one launch: the first
+// n_bns_ctas blocks run bound-and-split, then every block consumes emitted
+// sub-patches as they become ready
+void launch_frame_kernel(const DrawDev* draws, const int* root_prefix, int n_draws, const FrameDev& fr, const Queue& q,
+                         const SubPatches& sub, const Framebuffer& fb, float* mshade, BigQuad* big, long long big_cap,
+                         unsigned long long* ctrl, long long spin_limit, int grid, int n_bns_ctas, cudaStream_t s);
+int frame_kernel_grid(int PS);
 void launch_raster_big(const DrawDev* draws, const FrameDev& fr, const Framebuffer& fb, const BigQuad* big,
                        long long big_cap, unsigned long long* ctrl, cudaStream_t s);
 void launch_resolve(const DrawDev* draws, const FrameDev& fr, const SubPatches& sub, const Framebuffer& fb,

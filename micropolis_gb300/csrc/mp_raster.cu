@@ -21,13 +21,11 @@
 // per-pass structure (kernels/dice.cl, kernels/reyes.cl shade and sample)
 // with position, pixel, depth and colour grids in HBM; pass_resolve takes a
 // winning fragment's colour from this pass's colour grid.
-#include "mp_internal.h"
+#include "mp_bns_loop.cuh"
 
 namespace mp {
 
 namespace {
-
-__device__ __forceinline__ unsigned long long* cw(unsigned long long* ctrl, int w) { return ctrl + w * kCtrlStride; }
 
 constexpr int kFastCoord = 1 << 19;
 constexpr int kFastExtent = 1024;
@@ -166,156 +164,238 @@ struct FusedSmem {
     float ex[NS * NV], ey[NS * NV], ez[NS * NV];
 };
 
+// Dices, shades and rasterizes the n (<= NS) sub-patches at [base, base+n)
+// of the emitted list with the whole block; ends with a barrier.
+template <int PS>
+__device__ __forceinline__ void raster_group(FusedSmem<PS>& sm, long long base, int n, const DrawDev* __restrict__ draws,
+                                             const FrameDev& fr, const SubPatches& sub, const Framebuffer& fb,
+                                             float* __restrict__ mshade, BigQuad* big, long long big_cap,
+                                             unsigned long long* ctrl, const V3& light, long long& frags) {
+    using SM = FusedSmem<PS>;
+    constexpr int G = SM::G, NV = SM::NV, NQ = PS * PS, BPL = PS / 8, NB = SM::NB;
+    const int tid = threadIdx.x;
+    const int vmaxx = (fr.W << fr.shift) - 1, vmaxy = (fr.H << fr.shift) - 1;
+    if (tid < n) {
+        sm.range[tid] = sub.range[base + tid];
+        sm.meta[tid] = sub.meta[base + tid];
+        sm.zero[tid] = 0;
+    }
+    for (int i = tid; i < n * NB; i += kFusedThreads) {
+        int* b = sm.bound[i / NB][i % NB];
+        b[0] = vmaxx; b[1] = vmaxy; b[2] = 0; b[3] = 0;
+    }
+    __syncthreads();
+    for (int i = tid; i < n * 20; i += kFusedThreads) {
+        const int k = i / 20, c = i % 20;
+        const DrawDev& d = draws[sm.meta[k].y];
+        const int ncp = d.type == 0 ? 16 : 20;
+        if (c < ncp) sm.cp[k][c] = __ldg(d.cp + (size_t)sm.meta[k].x * ncp + c);
+    }
+    for (int i = tid; i < n * 32; i += kFusedThreads) {
+        const int k = i >> 5, c = i & 31;
+        const DrawDev& d = draws[sm.meta[k].y];
+        if (c < 16) sm.mv[k][c] = d.mv[c]; else sm.proj[k][c - 16] = d.proj[c - 16];
+        if (c == 0) { sm.type[k] = d.type; sm.view[k] = d.view; }
+    }
+    // dice parameters and Bernstein weights of each row / column of vertices
+    for (int i = tid; i < n * 2 * G; i += kFusedThreads) {
+        const int k = i / (2 * G), c = i % (2 * G);
+        const float4 rg = sm.range[k];
+        if (c < G) {
+            const float t = dice_param(rg.x, rg.z, c, fr);
+            sm.tx[k][c] = t;
+            sm.vw[k][c] = row_weights(t);
+        } else {
+            const float t = dice_param(rg.y, rg.w, c - G, fr);
+            sm.ty[k][c - G] = t;
+            sm.cw[k][c - G] = col_weights(t);
+        }
+    }
+    __syncthreads();
+    // dice vertices (kernels/dice.cl:37-80)
+    for (int i = tid; i < n * NV; i += kFusedThreads) {
+        const int k = i / NV, v = i % NV;
+        const int nu = v % G, nv = v / G;
+        float4 pos = dice_eye_w(sm.type[k], sm.mv[k], fr, sm.cp[k], sm.tx[k][nu], sm.ty[k][nv], sm.vw[k][nu],
+                                sm.cw[k][nv]);
+        int px, py;
+        float dep;
+        project_vertex_m(sm.proj[k], fr, pos, px, py, dep);
+        sm.px[i] = px;
+        sm.py[i] = py;
+        sm.dep[i] = dep;
+        sm.ex[i] = pos.x;
+        sm.ey[i] = pos.y;
+        sm.ez[i] = pos.z;
+        if (pos.z == 0.0f) {
+            // a vertex at eye z == 0 drops every 8x8 block it belongs to (kernels/reyes.cl:130-162)
+            unsigned zb = 0;
+            for (int bv = max(nv - 1, 0) / 8; bv <= min(nv, PS - 1) / 8; ++bv)
+                for (int bu = max(nu - 1, 0) / 8; bu <= min(nu, PS - 1) / 8; ++bu) zb |= 1u << (bu + bv * BPL);
+            atomicOr(&sm.zero[k], zb);
+        }
+    }
+    __syncthreads();
+    // block bounds over front-facing quads (kernels/reyes.cl:120-166)
+    for (int i = tid; i < n * NQ; i += kFusedThreads) {
+        const int k = i / NQ, q = i % NQ;
+        const int nu = q % PS, nv = q / PS, i0 = k * NV + nu + nv * G;
+        const int qx[4] = {sm.px[i0], sm.px[i0 + 1], sm.px[i0 + G], sm.px[i0 + G + 1]};
+        const int qy[4] = {sm.py[i0], sm.py[i0 + 1], sm.py[i0 + G], sm.py[i0 + G + 1]};
+        QuadBound qb = quad_block_bound(fr, qx, qy);
+        if (!qb.ff) { qb.pminx = vmaxx; qb.pminy = vmaxy; qb.pmaxx = 0; qb.pmaxy = 0; }
+        // lanes of one (sub-patch, block) reduce in registers, then one
+        // shared atomic per group (n * NQ is a multiple of 32: whole warps)
+        const unsigned grp = __match_any_sync(0xffffffffu, k * NB + (nu >> 3) + (nv >> 3) * BPL);
+        const int x0 = __reduce_min_sync(grp, qb.pminx), y0 = __reduce_min_sync(grp, qb.pminy);
+        const int x1 = __reduce_max_sync(grp, qb.pmaxx), y1 = __reduce_max_sync(grp, qb.pmaxy);
+        if ((tid & 31) == __ffs(grp) - 1) {
+            int* b = sm.bound[k][(nu >> 3) + (nv >> 3) * BPL];
+            atomicMin(b + 0, x0);
+            atomicMin(b + 1, y0);
+            atomicMax(b + 2, x1);
+            atomicMax(b + 3, y1);
+        }
+    }
+    __syncthreads();
+    // the tile range of each block, or a skip mark
+    for (int i = tid; i < n * NB; i += kFusedThreads) {
+        const int k = i / NB, b = i % NB;
+        const int* bb = sm.bound[k][b];
+        int* t = sm.tiles[k][b];
+        if (!block_tiles(fr, bb[0], bb[1], bb[2], bb[3], !((sm.zero[k] >> b) & 1), t)) {
+            t[0] = 1;
+            t[2] = 0;
+        }
+    }
+    __syncthreads();
+    // rasterize every quad of a live block
+    for (int i = tid; i < n * NQ; i += kFusedThreads) {
+        const int k = i / NQ, q = i % NQ;
+        const int nu = q % PS, nv = q / PS, blk = (nu >> 3) + (nv >> 3) * BPL;
+        const int* tp = sm.tiles[k][blk];
+        if (tp[0] > tp[2]) continue;
+        const int tiles[4] = {tp[0], tp[1], tp[2], tp[3]};
+        const int i0 = k * NV + nu + nv * G;
+        const int idx[4] = {i0, i0 + 1, i0 + G, i0 + G + 1};
+        int qx[4], qy[4];
+        float qd[4];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            qx[c] = sm.px[idx[c]];
+            qy[c] = sm.py[idx[c]];
+            qd[c] = sm.dep[idx[c]];
+        }
+        const long long s = base + k;
+        const unsigned mp_id = (unsigned)(s * NQ + nu + nv * PS);
+        const int view = sm.view[k];
+        unsigned long long* keys = fb.keys + (long long)view * fb.pixels;
+        int minx, miny, maxx, maxy, f = 0;
+        const bool fast = quad_is_fast(qx, qy, minx, miny, maxx, maxy);
+        if (fast)
+            f = raster_quad_fast(fr, keys, qx, qy, qd, minx, miny, maxx, maxy, mp_id);
+        else
+            push_big(big, big_cap, ctrl, qx, qy, qd, mp_id, view, tiles);
+        if (f > 0 || !fast) {
+            // the diffuse factor of a quad that may own pixels; resolve
+            // turns it into the colour of kernels/reyes.cl:191
+            mshade[mp_id] = shade_m_l(light, sm.ex[idx[0]], sm.ey[idx[0]], sm.ez[idx[0]], sm.ex[idx[1]], sm.ey[idx[1]],
+                                    sm.ez[idx[1]], sm.ex[idx[2]], sm.ey[idx[2]], sm.ez[idx[2]], sm.ex[idx[3]],
+                                    sm.ey[idx[3]], sm.ez[idx[3]]);
+        }
+        frags += f;
+    }
+    __syncthreads();
+}
+
 template <int PS>
 __global__ void __launch_bounds__(kFusedThreads, FusedCfg<PS>::MINB)
     raster_fused_kernel(const DrawDev* __restrict__ draws, FrameDev fr, SubPatches sub, Framebuffer fb,
                         float* __restrict__ mshade, BigQuad* big, long long big_cap, unsigned long long* ctrl) {
     using SM = FusedSmem<PS>;
-    constexpr int NS = SM::NS, G = SM::G, NV = SM::NV, NQ = PS * PS, BPL = PS / 8, NB = SM::NB;
+    constexpr int NS = SM::NS;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     SM& sm = *reinterpret_cast<SM*>(smem_raw);
-    const int tid = threadIdx.x;
     long long S = (long long)*(volatile unsigned long long*)cw(ctrl, kOutCount);
     if (S > sub.capacity) S = sub.capacity;
-    const int vmaxx = (fr.W << fr.shift) - 1, vmaxy = (fr.H << fr.shift) - 1;
     const V3 light = light_dir();
     long long frags = 0;
-    for (long long base = (long long)blockIdx.x * NS; base < S; base += (long long)gridDim.x * NS) {
-        const int n = (int)min((long long)NS, S - base);
-        if (tid < n) {
-            sm.range[tid] = sub.range[base + tid];
-            sm.meta[tid] = sub.meta[base + tid];
-            sm.zero[tid] = 0;
+    for (long long base = (long long)blockIdx.x * NS; base < S; base += (long long)gridDim.x * NS)
+        raster_group<PS>(sm, base, (int)min((long long)NS, S - base), draws, fr, sub, fb, mshade, big, big_cap, ctrl,
+                         light, frags);
+    frags = __reduce_add_sync(0xffffffffu, (unsigned)frags);
+    if ((threadIdx.x & 31) == 0 && frags) atomicAdd(cw(ctrl, kFragments), (unsigned long long)frags);
+}
+
+// One launch per frame: blocks [0, n_bns_ctas) first run the bound-and-split
+// warp loop (each emitted slot is marked with the frame's epoch); then every
+// block claims groups of NS consecutive emitted slots, waits (bounded) until
+// they are marked or lie beyond the final count, and rasterizes them.  The
+// grid is sized to what is resident at once, and the bound-and-split blocks
+// have the lowest indices, so the blocks that wait never wait on a block that
+// has not started; a wait that runs out stops consumption and reports
+// MP_ERR_TIMEOUT.
+template <int PS>
+__global__ void __launch_bounds__(kFusedThreads, 3)
+    frame_kernel(const DrawDev* __restrict__ gdraws, const int* __restrict__ root_prefix, int n_draws, FrameDev fr,
+                 Queue q, SubPatches sub, Framebuffer fb, float* __restrict__ mshade, BigQuad* big, long long big_cap,
+                 unsigned long long* ctrl, long long spin_limit, int n_bns_ctas) {
+    using SM = FusedSmem<PS>;
+    constexpr int NS = SM::NS;
+    constexpr int kStaged = (int)(sizeof(SM) / sizeof(DrawDev)) < 64 ? (int)(sizeof(SM) / sizeof(DrawDev)) : 64;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ long long s_group;
+    if ((int)blockIdx.x < n_bns_ctas) {
+        // draw constants staged in the (not yet used) raster buffer
+        DrawDev* sd = reinterpret_cast<DrawDev*>(smem_raw);
+        const bool staged = n_draws <= kStaged;
+        if (staged) {
+            const int words = n_draws * (int)(sizeof(DrawDev) / 4);
+            for (int i = threadIdx.x; i < words; i += blockDim.x)
+                reinterpret_cast<int*>(sd)[i] = __ldg(reinterpret_cast<const int*>(gdraws) + i);
+            __syncthreads();
         }
-        for (int i = tid; i < n * NB; i += kFusedThreads) {
-            int* b = sm.bound[i / NB][i % NB];
-            b[0] = vmaxx; b[1] = vmaxy; b[2] = 0; b[3] = 0;
-        }
-        __syncthreads();
-        for (int i = tid; i < n * 20; i += kFusedThreads) {
-            const int k = i / 20, c = i % 20;
-            const DrawDev& d = draws[sm.meta[k].y];
-            const int ncp = d.type == 0 ? 16 : 20;
-            if (c < ncp) sm.cp[k][c] = __ldg(d.cp + (size_t)sm.meta[k].x * ncp + c);
-        }
-        for (int i = tid; i < n * 32; i += kFusedThreads) {
-            const int k = i >> 5, c = i & 31;
-            const DrawDev& d = draws[sm.meta[k].y];
-            if (c < 16) sm.mv[k][c] = d.mv[c]; else sm.proj[k][c - 16] = d.proj[c - 16];
-            if (c == 0) { sm.type[k] = d.type; sm.view[k] = d.view; }
-        }
-        // dice parameters and Bernstein weights of each row / column of vertices
-        for (int i = tid; i < n * 2 * G; i += kFusedThreads) {
-            const int k = i / (2 * G), c = i % (2 * G);
-            const float4 rg = sm.range[k];
-            if (c < G) {
-                const float t = dice_param(rg.x, rg.z, c, fr);
-                sm.tx[k][c] = t;
-                sm.vw[k][c] = row_weights(t);
-            } else {
-                const float t = dice_param(rg.y, rg.w, c - G, fr);
-                sm.ty[k][c - G] = t;
-                sm.cw[k][c - G] = col_weights(t);
-            }
-        }
-        __syncthreads();
-        // dice vertices (kernels/dice.cl:37-80)
-        for (int i = tid; i < n * NV; i += kFusedThreads) {
-            const int k = i / NV, v = i % NV;
-            const int nu = v % G, nv = v / G;
-            float4 pos = dice_eye_w(sm.type[k], sm.mv[k], fr, sm.cp[k], sm.tx[k][nu], sm.ty[k][nv], sm.vw[k][nu],
-                                    sm.cw[k][nv]);
-            int px, py;
-            float dep;
-            project_vertex_m(sm.proj[k], fr, pos, px, py, dep);
-            sm.px[i] = px;
-            sm.py[i] = py;
-            sm.dep[i] = dep;
-            sm.ex[i] = pos.x;
-            sm.ey[i] = pos.y;
-            sm.ez[i] = pos.z;
-            if (pos.z == 0.0f) {
-                // a vertex at eye z == 0 drops every 8x8 block it belongs to (kernels/reyes.cl:130-162)
-                unsigned zb = 0;
-                for (int bv = max(nv - 1, 0) / 8; bv <= min(nv, PS - 1) / 8; ++bv)
-                    for (int bu = max(nu - 1, 0) / 8; bu <= min(nu, PS - 1) / 8; ++bu) zb |= 1u << (bu + bv * BPL);
-                atomicOr(&sm.zero[k], zb);
-            }
-        }
-        __syncthreads();
-        // block bounds over front-facing quads (kernels/reyes.cl:120-166)
-        for (int i = tid; i < n * NQ; i += kFusedThreads) {
-            const int k = i / NQ, q = i % NQ;
-            const int nu = q % PS, nv = q / PS, i0 = k * NV + nu + nv * G;
-            const int qx[4] = {sm.px[i0], sm.px[i0 + 1], sm.px[i0 + G], sm.px[i0 + G + 1]};
-            const int qy[4] = {sm.py[i0], sm.py[i0 + 1], sm.py[i0 + G], sm.py[i0 + G + 1]};
-            QuadBound qb = quad_block_bound(fr, qx, qy);
-            if (!qb.ff) { qb.pminx = vmaxx; qb.pminy = vmaxy; qb.pmaxx = 0; qb.pmaxy = 0; }
-            // lanes of one (sub-patch, block) reduce in registers, then one
-            // shared atomic per group (n * NQ is a multiple of 32: whole warps)
-            const unsigned grp = __match_any_sync(0xffffffffu, k * NB + (nu >> 3) + (nv >> 3) * BPL);
-            const int x0 = __reduce_min_sync(grp, qb.pminx), y0 = __reduce_min_sync(grp, qb.pminy);
-            const int x1 = __reduce_max_sync(grp, qb.pmaxx), y1 = __reduce_max_sync(grp, qb.pmaxy);
-            if ((tid & 31) == __ffs(grp) - 1) {
-                int* b = sm.bound[k][(nu >> 3) + (nv >> 3) * BPL];
-                atomicMin(b + 0, x0);
-                atomicMin(b + 1, y0);
-                atomicMax(b + 2, x1);
-                atomicMax(b + 3, y1);
-            }
-        }
-        __syncthreads();
-        // the tile range of each block, or a skip mark
-        for (int i = tid; i < n * NB; i += kFusedThreads) {
-            const int k = i / NB, b = i % NB;
-            const int* bb = sm.bound[k][b];
-            int* t = sm.tiles[k][b];
-            if (!block_tiles(fr, bb[0], bb[1], bb[2], bb[3], !((sm.zero[k] >> b) & 1), t)) {
-                t[0] = 1;
-                t[2] = 0;
-            }
-        }
-        __syncthreads();
-        // rasterize every quad of a live block
-        for (int i = tid; i < n * NQ; i += kFusedThreads) {
-            const int k = i / NQ, q = i % NQ;
-            const int nu = q % PS, nv = q / PS, blk = (nu >> 3) + (nv >> 3) * BPL;
-            const int* tp = sm.tiles[k][blk];
-            if (tp[0] > tp[2]) continue;
-            const int tiles[4] = {tp[0], tp[1], tp[2], tp[3]};
-            const int i0 = k * NV + nu + nv * G;
-            const int idx[4] = {i0, i0 + 1, i0 + G, i0 + G + 1};
-            int qx[4], qy[4];
-            float qd[4];
-#pragma unroll
-            for (int c = 0; c < 4; ++c) {
-                qx[c] = sm.px[idx[c]];
-                qy[c] = sm.py[idx[c]];
-                qd[c] = sm.dep[idx[c]];
-            }
-            const long long s = base + k;
-            const unsigned mp_id = (unsigned)(s * NQ + nu + nv * PS);
-            const int view = sm.view[k];
-            unsigned long long* keys = fb.keys + (long long)view * fb.pixels;
-            int minx, miny, maxx, maxy, f = 0;
-            const bool fast = quad_is_fast(qx, qy, minx, miny, maxx, maxy);
-            if (fast)
-                f = raster_quad_fast(fr, keys, qx, qy, qd, minx, miny, maxx, maxy, mp_id);
-            else
-                push_big(big, big_cap, ctrl, qx, qy, qd, mp_id, view, tiles);
-            if (f > 0 || !fast) {
-                // the diffuse factor of a quad that may own pixels; resolve
-                // turns it into the colour of kernels/reyes.cl:191
-                mshade[mp_id] = shade_m_l(light, sm.ex[idx[0]], sm.ey[idx[0]], sm.ez[idx[0]], sm.ex[idx[1]], sm.ey[idx[1]],
-                                        sm.ez[idx[1]], sm.ex[idx[2]], sm.ey[idx[2]], sm.ez[idx[2]], sm.ex[idx[3]],
-                                        sm.ey[idx[3]], sm.ez[idx[3]]);
-            }
-            frags += f;
-        }
+        bns_warp_loop(staged ? sd : gdraws, root_prefix, n_draws, fr, q, sub, sub.seq, ctrl, spin_limit);
         __syncthreads();
     }
+    SM& sm = *reinterpret_cast<SM*>(smem_raw);
+    const unsigned epoch = (unsigned)*(volatile unsigned long long*)cw(ctrl, kEpoch);
+    const V3 light = light_dir();
+    long long frags = 0;
+    while (true) {
+        if (threadIdx.x == 0) s_group = (long long)atomicAdd(cw(ctrl, kGroupTicket), 1ull);
+        __syncthreads();
+        const long long base = s_group * NS;
+        int ready = 0, gave_up = 0;
+        if ((int)threadIdx.x < NS) {
+            const long long slot = base + threadIdx.x;
+            long long idle = 0;
+            unsigned ns = 32;
+            while (true) {
+                if (slot < sub.capacity && ld_acquire_u32(sub.seq + slot) == epoch) {
+                    ready = 1;
+                    break;
+                }
+                if (ld_acquire_u64(cw(ctrl, kDone))) {
+                    // every emit's count update precedes the done flag
+                    const long long fin = (long long)atomicAdd(cw(ctrl, kOutCount), 0ull);
+                    if (slot >= fin || slot >= sub.capacity) break;  // beyond the end of the list
+                }
+                if (++idle > spin_limit) {
+                    set_status(ctrl, kErrTimeout);
+                    gave_up = 1;
+                    break;
+                }
+                __nanosleep(ns);
+                if (ns < 256) ns <<= 1;
+            }
+        }
+        const int n = __syncthreads_count(ready);
+        if (n == 0 || __syncthreads_or(gave_up)) break;
+        raster_group<PS>(sm, base, n, gdraws, fr, sub, fb, mshade, big, big_cap, ctrl, light, frags);
+    }
     frags = __reduce_add_sync(0xffffffffu, (unsigned)frags);
-    if ((tid & 31) == 0 && frags) atomicAdd(cw(ctrl, kFragments), (unsigned long long)frags);
+    if ((threadIdx.x & 31) == 0 && frags) atomicAdd(cw(ctrl, kFragments), (unsigned long long)frags);
 }
 
 // Exact replay of the reference's per-tile candidate loop for one quad
@@ -582,6 +662,17 @@ int fused_grid_impl() {
     return sms * per_sm;
 }
 
+template <int PS>
+int frame_grid_impl() {
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaFuncSetAttribute(frame_kernel<PS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(FusedSmem<PS>));
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, frame_kernel<PS>, kFusedThreads, sizeof(FusedSmem<PS>));
+    if (per_sm < 1) per_sm = 1;
+    return sms * per_sm;
+}
+
 int grid_for(long long n, int block) {
     long long g = (n + block - 1) / block;
     if (g < 1) g = 1;
@@ -609,6 +700,19 @@ void launch_raster_fused(const DrawDev* draws, const FrameDev& fr, const SubPatc
     else
         raster_fused_kernel<8><<<grid, kFusedThreads, sizeof(FusedSmem<8>), s>>>(draws, fr, sub, fb, mshade, big,
                                                                                 big_cap, ctrl);
+}
+
+int frame_kernel_grid(int PS) { return PS == 16 ? frame_grid_impl<16>() : frame_grid_impl<8>(); }
+
+void launch_frame_kernel(const DrawDev* draws, const int* root_prefix, int n_draws, const FrameDev& fr, const Queue& q,
+                         const SubPatches& sub, const Framebuffer& fb, float* mshade, BigQuad* big, long long big_cap,
+                         unsigned long long* ctrl, long long spin_limit, int grid, int n_bns_ctas, cudaStream_t s) {
+    if (fr.PS == 16)
+        frame_kernel<16><<<grid, kFusedThreads, sizeof(FusedSmem<16>), s>>>(
+            draws, root_prefix, n_draws, fr, q, sub, fb, mshade, big, big_cap, ctrl, spin_limit, n_bns_ctas);
+    else
+        frame_kernel<8><<<grid, kFusedThreads, sizeof(FusedSmem<8>), s>>>(
+            draws, root_prefix, n_draws, fr, q, sub, fb, mshade, big, big_cap, ctrl, spin_limit, n_bns_ctas);
 }
 
 void launch_raster_big(const DrawDev*, const FrameDev& fr, const Framebuffer& fb, const BigQuad* big,

@@ -32,6 +32,8 @@ class ReyesOptions:
     queue_capacity: int = 0                    # first-frame capacities (0 = automatic; they grow)
     subpatch_capacity: int = 0
     spin_limit: int = 0                        # bounded-wait iterations (0 = default)
+    overlap: bool = False                      # batched: rasterize while bound-and-split emits
+    bns_blocks: int = 0                        # batched overlap: blocks starting with bound-and-split (0 = auto)
 
     def update(self, **kw) -> "ReyesOptions":
         for k, v in kw.items():

@@ -70,6 +70,8 @@ class Renderer:
         o.subpatch_capacity = opts.subpatch_capacity
         if opts.spin_limit:
             o.spin_limit = opts.spin_limit
+        o.overlap = int(bool(opts.overlap))
+        o.bns_blocks = int(opts.bns_blocks)
         self._ctx = ctypes.c_void_p()
         st = lib().mp_create(ctypes.byref(o), ctypes.byref(self._ctx))
         if st != 0:
