@@ -69,6 +69,12 @@ typedef struct {
      * launches (0); bns_blocks = blocks that start with bound&split (0 = auto) */
     int32_t overlap;
     int32_t bns_blocks;
+    /* tuning knobs that do not change the image (0 = default):
+     * raster_tile: tile of the depth|id key buffer in pixels (8, 16, 32);
+     * dice_group: sub-patches diced together per 256-thread block
+     * (8, 16 or 22 at reyes_patch_size 8; 2, 4 or 6 at 16) */
+    int32_t raster_tile;
+    int32_t dice_group;
 } mp_options;
 
 /* The reference's Projection(fovy, near, viewport) (src/base/Projection.h:144). */

@@ -28,7 +28,8 @@ class MpOptions(ctypes.Structure):
                 ("displacement", ctypes.c_int32), ("displacement_amplitude", ctypes.c_float),
                 ("clear_color", ctypes.c_float * 4), ("batch_views", ctypes.c_int32), ("path", ctypes.c_int32),
                 ("queue_capacity", ctypes.c_int64), ("subpatch_capacity", ctypes.c_int64),
-                ("spin_limit", ctypes.c_int64), ("overlap", ctypes.c_int32), ("bns_blocks", ctypes.c_int32)]
+                ("spin_limit", ctypes.c_int64), ("overlap", ctypes.c_int32), ("bns_blocks", ctypes.c_int32),
+                ("raster_tile", ctypes.c_int32), ("dice_group", ctypes.c_int32)]
 
 
 class MpProjection(ctypes.Structure):

@@ -100,7 +100,9 @@ __global__ void __launch_bounds__(kAdjBlock) adjoint_kernel(const DrawDev* __res
     float gamp = 0.0f;
     const DrawDev* dp = nullptr;
     if (i < fb.pixels) {
-        unsigned long long key = fb.keys[(long long)view * fb.pixels + i];
+        int px, py;
+        fb_pixel(fr, i, px, py);
+        unsigned long long key = fb.keys[(long long)view * fb.key_pixels + key_index(fr, px, py)];
         if (key != kClearKey) {
             unsigned id = (unsigned)(key & 0xffffffffu);
             unsigned s = id / (unsigned)(PS * PS), q = id % (unsigned)(PS * PS);

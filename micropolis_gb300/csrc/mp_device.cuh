@@ -57,6 +57,8 @@ struct FrameDev {
     float clear[4];        // clear colour (powf(c, 2.2), alpha 1000)
     int gx, gy;            // 8-pixel tile grid of the output framebuffer
     int n_draws;
+    int kshift;            // depth|id key buffer tile: 1 << kshift pixels (8, 16 or 32)
+    int kgx;               // key tiles per row
     int pad1;
 };
 
@@ -533,6 +535,18 @@ __device__ __forceinline__ unsigned idepth_of(float depth) {
 __device__ __forceinline__ long long fb_index(const FrameDev& fr, int x, int y) {
     int tx = x >> 3, ty = y >> 3;
     return ((long long)(tx + fr.gx * ty) << 6) + (x & 7) + ((y & 7) << 3);
+}
+// Pixel of output index i (inverse of fb_index).
+__device__ __forceinline__ void fb_pixel(const FrameDev& fr, long long i, int& x, int& y) {
+    const int t = (int)(i >> 6);
+    x = ((t % fr.gx) << 3) + (int)(i & 7);
+    y = ((t / fr.gx) << 3) + (int)((i >> 3) & 7);
+}
+// Index of pixel (x, y) in the depth|id key buffer, tiled by 1 << kshift
+// pixels so that the atomics of one micropolygon neighbourhood share lines.
+__device__ __forceinline__ long long key_index(const FrameDev& fr, int x, int y) {
+    const int k = fr.kshift, m = (1 << k) - 1;
+    return ((long long)((x >> k) + fr.kgx * (y >> k)) << (2 * k)) + (x & m) + ((y & m) << k);
 }
 
 }  // namespace mp

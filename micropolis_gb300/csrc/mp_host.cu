@@ -381,12 +381,12 @@ int bns_blocks(const mp_ctx* c) {
 void launch_middle(mp_ctx* c, int n) {
     if (c->opt.overlap) {
         launch_frame_kernel(c->d_draws, c->d_root_prefix, n, c->fr, c->q, c->sub, c->fb, c->mshade, c->big, c->big_cap,
-                            c->ctrl, c->opt.spin_limit, c->frame_grid, bns_blocks(c), c->stream);
+                            c->ctrl, c->opt.spin_limit, c->frame_grid, bns_blocks(c), c->opt.dice_group, c->stream);
     } else {
         launch_bns_persistent(c->d_draws, c->d_root_prefix, n, c->fr, c->q, c->sub, c->ctrl, c->bns_grid,
                               c->opt.spin_limit, c->stream);
         launch_raster_fused(c->d_draws, c->fr, c->sub, c->fb, c->mshade, c->big, c->big_cap, c->ctrl, c->raster_grid,
-                            c->stream);
+                            c->opt.dice_group, c->stream);
     }
 }
 
@@ -456,7 +456,7 @@ mp_status batched_frame(mp_ctx* c) {
                                       c->opt.spin_limit, c->stream);
                 CK(cudaEventRecord(c->sev[1], c->stream));
                 launch_raster_fused(c->d_draws, c->fr, c->sub, c->fb, c->mshade, c->big, c->big_cap, c->ctrl,
-                                    c->raster_grid, c->stream);
+                                    c->raster_grid, c->opt.dice_group, c->stream);
             }
             CK(cudaEventRecord(c->sev[2], c->stream));
             launch_raster_big(c->d_draws, c->fr, c->fb, c->big, c->big_cap, c->ctrl, c->stream);
@@ -595,6 +595,13 @@ mp_status mp_create(const mp_options* opts, mp_ctx** out) {
     if (o.reyes_patches_per_pass < 1 || o.batch_views < 1 || o.batch_views > 65536) return MP_ERR_INVALID_ARG;
     if (o.path != MP_PATH_PLAIN && o.path != MP_PATH_BATCHED) return MP_ERR_INVALID_ARG;
     if (o.spin_limit <= 0) o.spin_limit = 1 << 20;
+    if (o.raster_tile == 0) o.raster_tile = 8;
+    if (o.raster_tile != 8 && o.raster_tile != 16 && o.raster_tile != 32) return MP_ERR_INVALID_ARG;
+    if (o.dice_group == 0) o.dice_group = o.reyes_patch_size == 16 ? 6 : 22;
+    if (o.reyes_patch_size == 8 && o.dice_group != 8 && o.dice_group != 16 && o.dice_group != 22)
+        return MP_ERR_INVALID_ARG;
+    if (o.reyes_patch_size == 16 && o.dice_group != 2 && o.dice_group != 4 && o.dice_group != 6)
+        return MP_ERR_INVALID_ARG;
     mp_ctx* c = new mp_ctx();
     c->opt = o;
     cudaError_t e = cudaGetDevice(&c->device);
@@ -632,7 +639,11 @@ mp_status mp_create(const mp_options* opts, mp_ctx** out) {
     ck(cudaMallocHost((void**)&c->h_ctrl, sizeof(unsigned long long) * kNumCtrl * kCtrlStride), "h_ctrl");
     c->fb.pixels = (long long)W * H;
     c->fb.views = o.batch_views;
-    ck(dalloc(&c->fb.keys, c->fb.pixels * c->fb.views), "fb keys");
+    // the key buffer is sized for the largest key tile (32 px) so the tile can change per frame
+    c->fb.key_pixels = (long long)((W + 31) / 32 * 32) * ((H + 31) / 32 * 32);
+    fr.kshift = o.raster_tile == 32 ? 5 : o.raster_tile == 16 ? 4 : 3;
+    fr.kgx = (W + (1 << fr.kshift) - 1) >> fr.kshift;
+    ck(dalloc(&c->fb.keys, c->fb.key_pixels * c->fb.views), "fb keys");
     ck(dalloc(&c->fb.color, c->fb.pixels * c->fb.views), "fb color");
     ck(dalloc(&c->fb.depth, c->fb.pixels * c->fb.views), "fb depth");
     ck(cudaEventCreate(&c->ev0), "event");
@@ -642,8 +653,8 @@ mp_status mp_create(const mp_options* opts, mp_ctx** out) {
     if (st == MP_OK) st = grow_big(c, 1 << 16);
     if (st == MP_OK) {
         c->bns_grid = bns_persistent_grid();
-        c->raster_grid = raster_fused_grid(fr.PS);
-        c->frame_grid = frame_kernel_grid(fr.PS);
+        c->raster_grid = raster_fused_grid(fr.PS, o.dice_group);
+        c->frame_grid = frame_kernel_grid(fr.PS, o.dice_group);
         launch_clear(c->fb, c->fr, 1, c->stream);
         ck(cudaStreamSynchronize(c->stream), "init");
     }
@@ -933,13 +944,19 @@ mp_status mp_copy_framebuffer_device(mp_ctx* c, int32_t view, void* color_dev, v
 mp_status mp_read_visibility(mp_ctx* c, int32_t view, int64_t* ids) {
     if (!c || !ids || view < 0 || view >= c->fb.views) return MP_ERR_INVALID_ARG;
     if (!c->frame_valid) return fail(c, MP_ERR_STATE, "no finished frame");
-    const long long n = c->fb.pixels;
-    std::vector<unsigned long long> k((size_t)n);
-    CK(cudaMemcpyAsync(k.data(), c->fb.keys + view * n, sizeof(unsigned long long) * (size_t)n,
+    const long long nk = c->fb.key_pixels;
+    std::vector<unsigned long long> k((size_t)nk);
+    CK(cudaMemcpyAsync(k.data(), c->fb.keys + view * nk, sizeof(unsigned long long) * (size_t)nk,
                        cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
-    for (long long i = 0; i < n; ++i)
-        ids[i] = k[(size_t)i] == kClearKey ? -1 : (int64_t)(k[(size_t)i] & 0xffffffffull);
+    const int W = c->fr.W, H = c->fr.H, ks = c->fr.kshift, m = (1 << ks) - 1;
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x) {
+            const long long o = ((long long)(x / 8 + c->fr.gx * (y / 8)) << 6) + (x & 7) + ((y & 7) << 3);
+            const long long ki = ((long long)((x >> ks) + c->fr.kgx * (y >> ks)) << (2 * ks)) + (x & m) + ((y & m) << ks);
+            const unsigned long long key = k[(size_t)ki];
+            ids[o] = key == kClearKey ? -1 : (int64_t)(key & 0xffffffffull);
+        }
     return MP_OK;
 }
 

@@ -57,7 +57,8 @@ struct Framebuffer {
     unsigned long long* keys;   // (idepth << 32 | mp_id) per pixel, tiled, per view
     float4* color;              // tiled colour, per view
     int* depth;                 // tiled int depth, per view
-    long long pixels;           // W * H
+    long long pixels;           // W * H (colour / depth per view)
+    long long key_pixels;       // key buffer per view (whole key tiles)
     int views;
 };
 
@@ -83,16 +84,17 @@ long long scan_state_words(long long n);
 // ---- dice / shade / raster / resolve (mp_raster.cu)
 void launch_clear(const Framebuffer& fb, const FrameDev& fr, int with_color, cudaStream_t s);
 void launch_raster_fused(const DrawDev* draws, const FrameDev& fr, const SubPatches& sub, const Framebuffer& fb,
-                         float* mshade, BigQuad* big, long long big_cap, unsigned long long* ctrl, int grid,
+                         float* mshade, BigQuad* big, long long big_cap, unsigned long long* ctrl, int grid, int group,
                          cudaStream_t s);
-int raster_fused_grid(int PS);
+int raster_fused_grid(int PS, int group);
 // bound-and-split and rasterization overlapped in one launch: the first
 // n_bns_ctas blocks run bound-and-split, then every block consumes emitted
 // sub-patches as they become ready
 void launch_frame_kernel(const DrawDev* draws, const int* root_prefix, int n_draws, const FrameDev& fr, const Queue& q,
                          const SubPatches& sub, const Framebuffer& fb, float* mshade, BigQuad* big, long long big_cap,
-                         unsigned long long* ctrl, long long spin_limit, int grid, int n_bns_ctas, cudaStream_t s);
-int frame_kernel_grid(int PS);
+                         unsigned long long* ctrl, long long spin_limit, int grid, int n_bns_ctas, int group,
+                         cudaStream_t s);
+int frame_kernel_grid(int PS, int group);
 void launch_raster_big(const DrawDev* draws, const FrameDev& fr, const Framebuffer& fb, const BigQuad* big,
                        long long big_cap, unsigned long long* ctrl, cudaStream_t s);
 void launch_resolve(const DrawDev* draws, const FrameDev& fr, const SubPatches& sub, const Framebuffer& fb,

@@ -108,7 +108,7 @@ __device__ __forceinline__ int raster_quad_fast(const FrameDev& fr, unsigned lon
             bool in2 = tri_test(t2, tx, ty, depth);
             if (in1 || in2) {
                 unsigned long long key = ((unsigned long long)idepth_of(depth) << 32) | mp_id;
-                atomicMin(keys + fb_index(fr, x, y), key);
+                atomicMin(keys + key_index(fr, x, y), key);
                 ++frags;
             }
         }
@@ -141,13 +141,10 @@ __device__ __forceinline__ void push_big(BigQuad* big, long long big_cap, unsign
 // NS * (PS+1)^2 dice vertices are spread over all threads (22 * 81 = 1782 =
 // 7 rounds of 256 at PS = 8), then the block bounds, then one thread per quad.
 constexpr int kFusedThreads = 256;
-template <int PS> struct FusedCfg;
-template <> struct FusedCfg<8> { static constexpr int NS = 22; static constexpr int MINB = 3; };
-template <> struct FusedCfg<16> { static constexpr int NS = 6; static constexpr int MINB = 3; };
 
-template <int PS>
+template <int PS, int NS_>
 struct FusedSmem {
-    static constexpr int NS = FusedCfg<PS>::NS, G = PS + 1, NV = G * G, NB = (PS / 8) * (PS / 8);
+    static constexpr int NS = NS_, G = PS + 1, NV = G * G, NB = (PS / 8) * (PS / 8);
     float4 cp[NS][20];
     float mv[NS][16];
     float proj[NS][16];
@@ -166,12 +163,12 @@ struct FusedSmem {
 
 // Dices, shades and rasterizes the n (<= NS) sub-patches at [base, base+n)
 // of the emitted list with the whole block; ends with a barrier.
-template <int PS>
-__device__ __forceinline__ void raster_group(FusedSmem<PS>& sm, long long base, int n, const DrawDev* __restrict__ draws,
+template <int PS, int NS>
+__device__ __forceinline__ void raster_group(FusedSmem<PS, NS>& sm, long long base, int n, const DrawDev* __restrict__ draws,
                                              const FrameDev& fr, const SubPatches& sub, const Framebuffer& fb,
                                              float* __restrict__ mshade, BigQuad* big, long long big_cap,
                                              unsigned long long* ctrl, const V3& light, long long& frags) {
-    using SM = FusedSmem<PS>;
+    using SM = FusedSmem<PS, NS>;
     constexpr int G = SM::G, NV = SM::NV, NQ = PS * PS, BPL = PS / 8, NB = SM::NB;
     const int tid = threadIdx.x;
     const int vmaxx = (fr.W << fr.shift) - 1, vmaxy = (fr.H << fr.shift) - 1;
@@ -289,7 +286,7 @@ __device__ __forceinline__ void raster_group(FusedSmem<PS>& sm, long long base, 
         const long long s = base + k;
         const unsigned mp_id = (unsigned)(s * NQ + nu + nv * PS);
         const int view = sm.view[k];
-        unsigned long long* keys = fb.keys + (long long)view * fb.pixels;
+        unsigned long long* keys = fb.keys + (long long)view * fb.key_pixels;
         int minx, miny, maxx, maxy, f = 0;
         const bool fast = quad_is_fast(qx, qy, minx, miny, maxx, maxy);
         if (fast)
@@ -308,12 +305,11 @@ __device__ __forceinline__ void raster_group(FusedSmem<PS>& sm, long long base, 
     __syncthreads();
 }
 
-template <int PS>
-__global__ void __launch_bounds__(kFusedThreads, FusedCfg<PS>::MINB)
+template <int PS, int NS>
+__global__ void __launch_bounds__(kFusedThreads, 3)
     raster_fused_kernel(const DrawDev* __restrict__ draws, FrameDev fr, SubPatches sub, Framebuffer fb,
                         float* __restrict__ mshade, BigQuad* big, long long big_cap, unsigned long long* ctrl) {
-    using SM = FusedSmem<PS>;
-    constexpr int NS = SM::NS;
+    using SM = FusedSmem<PS, NS>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     SM& sm = *reinterpret_cast<SM*>(smem_raw);
     long long S = (long long)*(volatile unsigned long long*)cw(ctrl, kOutCount);
@@ -321,8 +317,8 @@ __global__ void __launch_bounds__(kFusedThreads, FusedCfg<PS>::MINB)
     const V3 light = light_dir();
     long long frags = 0;
     for (long long base = (long long)blockIdx.x * NS; base < S; base += (long long)gridDim.x * NS)
-        raster_group<PS>(sm, base, (int)min((long long)NS, S - base), draws, fr, sub, fb, mshade, big, big_cap, ctrl,
-                         light, frags);
+        raster_group<PS, NS>(sm, base, (int)min((long long)NS, S - base), draws, fr, sub, fb, mshade, big, big_cap,
+                             ctrl, light, frags);
     frags = __reduce_add_sync(0xffffffffu, (unsigned)frags);
     if ((threadIdx.x & 31) == 0 && frags) atomicAdd(cw(ctrl, kFragments), (unsigned long long)frags);
 }
@@ -335,13 +331,12 @@ __global__ void __launch_bounds__(kFusedThreads, FusedCfg<PS>::MINB)
 // have the lowest indices, so the blocks that wait never wait on a block that
 // has not started; a wait that runs out stops consumption and reports
 // MP_ERR_TIMEOUT.
-template <int PS>
+template <int PS, int NS>
 __global__ void __launch_bounds__(kFusedThreads, 3)
     frame_kernel(const DrawDev* __restrict__ gdraws, const int* __restrict__ root_prefix, int n_draws, FrameDev fr,
                  Queue q, SubPatches sub, Framebuffer fb, float* __restrict__ mshade, BigQuad* big, long long big_cap,
                  unsigned long long* ctrl, long long spin_limit, int n_bns_ctas) {
-    using SM = FusedSmem<PS>;
-    constexpr int NS = SM::NS;
+    using SM = FusedSmem<PS, NS>;
     constexpr int kStaged = (int)(sizeof(SM) / sizeof(DrawDev)) < 64 ? (int)(sizeof(SM) / sizeof(DrawDev)) : 64;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ long long s_group;
@@ -392,7 +387,7 @@ __global__ void __launch_bounds__(kFusedThreads, 3)
         }
         const int n = __syncthreads_count(ready);
         if (n == 0 || __syncthreads_or(gave_up)) break;
-        raster_group<PS>(sm, base, n, gdraws, fr, sub, fb, mshade, big, big_cap, ctrl, light, frags);
+        raster_group<PS, NS>(sm, base, n, gdraws, fr, sub, fb, mshade, big, big_cap, ctrl, light, frags);
     }
     frags = __reduce_add_sync(0xffffffffu, (unsigned)frags);
     if ((threadIdx.x & 31) == 0 && frags) atomicAdd(cw(ctrl, kFragments), (unsigned long long)frags);
@@ -446,7 +441,7 @@ __global__ void __launch_bounds__(kBigThreads) raster_big_kernel(FrameDev fr, Fr
         Tri t1, t2;
         tri_setup(t1, b.px[0], b.py[0], b.depth[0], b.px[1], b.py[1], b.depth[1], b.px[3], b.py[3], b.depth[3]);
         tri_setup(t2, b.px[0], b.py[0], b.depth[0], b.px[3], b.py[3], b.depth[3], b.px[2], b.py[2], b.depth[2]);
-        unsigned long long* keys = fb.keys + (long long)b.view * fb.pixels;
+        unsigned long long* keys = fb.keys + (long long)b.view * fb.key_pixels;
         long long total = (long long)s_nx * s_ny;
         int frags = 0;
         for (long long c = threadIdx.x; c < total; c += kBigThreads) {
@@ -457,7 +452,7 @@ __global__ void __launch_bounds__(kBigThreads) raster_big_kernel(FrameDev fr, Fr
             bool in2 = tri_test(t2, tx, ty, depth);
             if (in1 || in2) {
                 unsigned long long key = ((unsigned long long)idepth_of(depth) << 32) | b.mp_id;
-                atomicMin(keys + fb_index(fr, x, y), key);
+                atomicMin(keys + key_index(fr, x, y), key);
                 ++frags;
             }
         }
@@ -470,15 +465,23 @@ __global__ void __launch_bounds__(kBigThreads) raster_big_kernel(FrameDev fr, Fr
 }
 
 __global__ void clear_kernel(Framebuffer fb, FrameDev fr, int with_color) {
-    long long n = fb.pixels * fb.views;
-    float4 cc = make_float4(fr.clear[0], fr.clear[1], fr.clear[2], fr.clear[3]);
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        fb.keys[i] = kClearKey;
-        if (with_color) {
+    const long long nk = fb.key_pixels * fb.views, n = fb.pixels * fb.views;
+    const float4 cc = make_float4(fr.clear[0], fr.clear[1], fr.clear[2], fr.clear[3]);
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nk; i += stride) fb.keys[i] = kClearKey;
+    if (with_color)
+        for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
             fb.color[i] = cc;
             fb.depth[i] = 0x7fffffff;
         }
-    }
+}
+
+// Key of output pixel i (all views).
+__device__ __forceinline__ unsigned long long key_of(const FrameDev& fr, const Framebuffer& fb, long long i) {
+    const long long v = i / fb.pixels;
+    int x, y;
+    fb_pixel(fr, i - v * fb.pixels, x, y);
+    return fb.keys[v * fb.key_pixels + key_index(fr, x, y)];
 }
 
 // Colour of each pixel from its winning micropolygon: the diffuse factor the
@@ -489,7 +492,7 @@ __global__ void resolve_kernel(const DrawDev* __restrict__ draws, FrameDev fr, S
                                const float* __restrict__ mshade) {
     long long n = fb.pixels * fb.views;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        unsigned long long key = fb.keys[i];
+        const unsigned long long key = key_of(fr, fb, i);
         if (key == kClearKey) {
             fb.color[i] = make_float4(fr.clear[0], fr.clear[1], fr.clear[2], fr.clear[3]);
             fb.depth[i] = 0x7fffffff;
@@ -603,7 +606,7 @@ __global__ void sample_grid_kernel(const DrawDev* __restrict__ draws, FrameDev f
                 qd[k] = depth_grid[idx[k]];
             }
             const int view = draws[sub.meta[base + s].y].view;
-            unsigned long long* keys = fb.keys + (long long)view * fb.pixels;
+            unsigned long long* keys = fb.keys + (long long)view * fb.key_pixels;
             unsigned mp_id = (unsigned)((base + s) * PS * PS + nu + nv * PS);
             int minx, miny, maxx, maxy;
             if (quad_is_fast(qx, qy, minx, miny, maxx, maxy))
@@ -621,8 +624,8 @@ __global__ void pass_resolve_kernel(FrameDev fr, Framebuffer fb, unsigned long l
                                     const float4* color_grid) {
     long long n = fb.pixels * fb.views;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        unsigned long long key = fb.keys[i];
-        unsigned long long id = key & 0xffffffffull;
+        const unsigned long long key = key_of(fr, fb, i);
+        const unsigned long long id = key & 0xffffffffull;
         if (key != kClearKey && id >= id_lo && id < id_hi) {
             fb.color[i] = color_grid[id - id_lo];
             fb.depth[i] = (int)(key >> 32);
@@ -649,28 +652,33 @@ __global__ void atomic_bench_kernel(unsigned long long* buf, long long n_slots, 
     }
 }
 
-template <int PS>
-int fused_grid_impl() {
+template <typename K>
+int resident_grid(K kernel, size_t smem) {
     int dev = 0, sms = 0, per_sm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaFuncSetAttribute(raster_fused_kernel<PS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)sizeof(FusedSmem<PS>));
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, raster_fused_kernel<PS>, kFusedThreads,
-                                                  sizeof(FusedSmem<PS>));
+    cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kFusedThreads, smem);
     if (per_sm < 1) per_sm = 1;
     return sms * per_sm;
 }
 
-template <int PS>
-int frame_grid_impl() {
-    int dev = 0, sms = 0, per_sm = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaFuncSetAttribute(frame_kernel<PS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(FusedSmem<PS>));
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, frame_kernel<PS>, kFusedThreads, sizeof(FusedSmem<PS>));
-    if (per_sm < 1) per_sm = 1;
-    return sms * per_sm;
+// Calls f(kernel instantiation tag) for the (PS, dice_group) pair.
+template <int PS, int NS>
+struct Tag {
+    static constexpr int ps = PS, ns = NS;
+};
+template <typename F>
+void dispatch_group(int PS, int group, F&& f) {
+    if (PS == 16) {
+        if (group == 2) f(Tag<16, 2>{});
+        else if (group == 4) f(Tag<16, 4>{});
+        else f(Tag<16, 6>{});
+    } else {
+        if (group == 8) f(Tag<8, 8>{});
+        else if (group == 16) f(Tag<8, 16>{});
+        else f(Tag<8, 22>{});
+    }
 }
 
 int grid_for(long long n, int block) {
@@ -686,33 +694,46 @@ int grid_for(long long n, int block) {
 // launchers
 
 void launch_clear(const Framebuffer& fb, const FrameDev& fr, int with_color, cudaStream_t s) {
-    clear_kernel<<<grid_for(fb.pixels * fb.views, 256), 256, 0, s>>>(fb, fr, with_color);
+    clear_kernel<<<grid_for(fb.key_pixels * fb.views, 256), 256, 0, s>>>(fb, fr, with_color);
 }
 
-int raster_fused_grid(int PS) { return PS == 16 ? fused_grid_impl<16>() : fused_grid_impl<8>(); }
+int raster_fused_grid(int PS, int group) {
+    int g = 0;
+    dispatch_group(PS, group, [&](auto t) {
+        using T = decltype(t);
+        g = resident_grid(raster_fused_kernel<T::ps, T::ns>, sizeof(FusedSmem<T::ps, T::ns>));
+    });
+    return g;
+}
 
 void launch_raster_fused(const DrawDev* draws, const FrameDev& fr, const SubPatches& sub, const Framebuffer& fb,
-                         float* mshade, BigQuad* big, long long big_cap, unsigned long long* ctrl, int grid,
+                         float* mshade, BigQuad* big, long long big_cap, unsigned long long* ctrl, int grid, int group,
                          cudaStream_t s) {
-    if (fr.PS == 16)
-        raster_fused_kernel<16><<<grid, kFusedThreads, sizeof(FusedSmem<16>), s>>>(draws, fr, sub, fb, mshade, big,
-                                                                                  big_cap, ctrl);
-    else
-        raster_fused_kernel<8><<<grid, kFusedThreads, sizeof(FusedSmem<8>), s>>>(draws, fr, sub, fb, mshade, big,
-                                                                                big_cap, ctrl);
+    dispatch_group(fr.PS, group, [&](auto t) {
+        using T = decltype(t);
+        raster_fused_kernel<T::ps, T::ns><<<grid, kFusedThreads, sizeof(FusedSmem<T::ps, T::ns>), s>>>(
+            draws, fr, sub, fb, mshade, big, big_cap, ctrl);
+    });
 }
 
-int frame_kernel_grid(int PS) { return PS == 16 ? frame_grid_impl<16>() : frame_grid_impl<8>(); }
+int frame_kernel_grid(int PS, int group) {
+    int g = 0;
+    dispatch_group(PS, group, [&](auto t) {
+        using T = decltype(t);
+        g = resident_grid(frame_kernel<T::ps, T::ns>, sizeof(FusedSmem<T::ps, T::ns>));
+    });
+    return g;
+}
 
 void launch_frame_kernel(const DrawDev* draws, const int* root_prefix, int n_draws, const FrameDev& fr, const Queue& q,
                          const SubPatches& sub, const Framebuffer& fb, float* mshade, BigQuad* big, long long big_cap,
-                         unsigned long long* ctrl, long long spin_limit, int grid, int n_bns_ctas, cudaStream_t s) {
-    if (fr.PS == 16)
-        frame_kernel<16><<<grid, kFusedThreads, sizeof(FusedSmem<16>), s>>>(
+                         unsigned long long* ctrl, long long spin_limit, int grid, int n_bns_ctas, int group,
+                         cudaStream_t s) {
+    dispatch_group(fr.PS, group, [&](auto t) {
+        using T = decltype(t);
+        frame_kernel<T::ps, T::ns><<<grid, kFusedThreads, sizeof(FusedSmem<T::ps, T::ns>), s>>>(
             draws, root_prefix, n_draws, fr, q, sub, fb, mshade, big, big_cap, ctrl, spin_limit, n_bns_ctas);
-    else
-        frame_kernel<8><<<grid, kFusedThreads, sizeof(FusedSmem<8>), s>>>(
-            draws, root_prefix, n_draws, fr, q, sub, fb, mshade, big, big_cap, ctrl, spin_limit, n_bns_ctas);
+    });
 }
 
 void launch_raster_big(const DrawDev*, const FrameDev& fr, const Framebuffer& fb, const BigQuad* big,

@@ -34,6 +34,8 @@ class ReyesOptions:
     spin_limit: int = 0                        # bounded-wait iterations (0 = default)
     overlap: bool = False                      # batched: rasterize while bound-and-split emits
     bns_blocks: int = 0                        # batched overlap: blocks starting with bound-and-split (0 = auto)
+    raster_tile: int = 0                       # depth|id key buffer tile in pixels (0 = 8)
+    dice_group: int = 0                        # sub-patches per fused 256-thread block (0 = default)
 
     def update(self, **kw) -> "ReyesOptions":
         for k, v in kw.items():

@@ -72,6 +72,8 @@ class Renderer:
             o.spin_limit = opts.spin_limit
         o.overlap = int(bool(opts.overlap))
         o.bns_blocks = int(opts.bns_blocks)
+        o.raster_tile = int(opts.raster_tile)
+        o.dice_group = int(opts.dice_group)
         self._ctx = ctypes.c_void_p()
         st = lib().mp_create(ctypes.byref(o), ctypes.byref(self._ctx))
         if st != 0:
