@@ -35,6 +35,10 @@ WORKLOAD = "mixed4096_1920x1080"
 METRIC = "micropolygons/s (batched path, 4096-patch mixed Bezier/Gregory scene, 1920x1080)"
 L2_FLUSH_BYTES = 256 << 20
 
+# DRAM bytes (read + write) per launch of each stage's kernel, from the ncu
+# capture summarised in profiles/ (dram__bytes_read.sum + dram__bytes_write.sum)
+NCU_TRAFFIC = {}
+
 
 def parse():
     ap = argparse.ArgumentParser()
@@ -124,13 +128,11 @@ def _cpu_chunk(args):
     return st["micropolygons"], time.perf_counter() - t
 
 
-def cpu_baseline(name: str, procs: int, patches_per_proc: int):
+def cpu_baseline(name: str, procs: int, patches_per_proc: int, pool=None):
     """micropolygons/s of the oracle path on `procs` processes, each rendering
-    its own disjoint slice of every draw's patches (a bounded sample)."""
-    import multiprocessing as mp
+    its own slice of every draw's patches (a bounded sample).  Returns
+    (rate, micropolygons, wall s, busiest process s)."""
     from micropolis_gb300 import scenes
-    from oracle import oracle
-    oracle.lib()
     sc = scenes.WORKLOADS[name]()
     jobs = []
     for p in range(procs):
@@ -141,15 +143,21 @@ def cpu_baseline(name: str, procs: int, patches_per_proc: int):
             sl.append((a, min(a + share, d.mesh.n_patches)))
         jobs.append((name, sl))
     t = time.perf_counter()
-    if procs == 1:
-        res = [_cpu_chunk(jobs[0])]
+    if pool is None:
+        res = [_cpu_chunk(j) for j in jobs]
     else:
-        with mp.get_context("spawn").Pool(procs) as pool:
-            res = pool.map(_cpu_chunk, jobs)
+        res = pool.map(_cpu_chunk, jobs)
     wall = time.perf_counter() - t
     mpoly = sum(r[0] for r in res)
     busy = max(r[1] for r in res)
     return mpoly / busy, mpoly, wall, busy
+
+
+def cpu_pool(procs: int):
+    """Worker processes for the CPU legs, started with spawn (never forked
+    from a process that has touched the GPU)."""
+    import multiprocessing as mp
+    return mp.get_context("spawn").Pool(procs)
 
 
 # --------------------------------------------------------------------------
@@ -159,12 +167,15 @@ def run_reference(args):
     if rank != 0:
         return 0
     cores = os.cpu_count() or 1
-    per = 96
+    # one step = one whole frame's 4096 patches shared over the cores
+    per = max(1, 4096 // cores)
     vals = []
-    for i in range(args.warmup + args.steps):
-        v, mpoly, wall, busy = cpu_baseline(WORKLOAD, cores, per)
-        if i >= args.warmup:
-            vals.append((v, mpoly, busy))
+    with cpu_pool(cores) as pool:
+        pool.map(_cpu_chunk, [(WORKLOAD, [(0, 1), (0, 1)])] * cores)   # import and build in every worker
+        for i in range(args.warmup + args.steps):
+            v, mpoly, wall, busy = cpu_baseline(WORKLOAD, cores, per, pool)
+            if i >= args.warmup:
+                vals.append((v, mpoly, busy))
     value = sum(v[1] for v in vals) / sum(v[2] for v in vals)
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "micropolygons/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(v[2] for v in vals),
@@ -172,11 +183,42 @@ def run_reference(args):
             "data": "synthetic (seeded generator, no dataset)",
             "config": {"workload": WORKLOAD, "sample": f"{cores} processes x {per} patches per step"},
             "cpu_baseline": {"value": value, "unit": "micropolygons/s", "cores": cores, "kind": "port",
-                             "sample": f"{cores} processes, each bound&split+dice+shade+sample of {per} of the "
-                                       f"4096 patches per step; CPU bound&split single-threaded per process"},
+                             "sample": f"one frame per step: {cores} processes, each bound&split+dice+shade+sample "
+                                       f"of {per} of the 4096 patches; bound&split single-threaded per process"},
             "e2e": {"value": value, "unit": "micropolygons/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
     return 0
+
+
+def views64_leg(stream):
+    """64 independent 512x512 scenes (100..10000 patches each) in one batched
+    frame with the tuned knobs, against the plain per-pass path drawing the
+    same 64 layers."""
+    import torch
+    from micropolis_gb300 import autotune, scenes
+    from micropolis_gb300.renderer import render_scene, renderer_for
+    sc = scenes.views64_512x512()
+    best = autotune.tune(sc, frames=3, warmup=1, use_cache=False)
+    out = {"patches": sc.n_patches, "views": 64, "tuned": best.best}
+    for path, over in (("batched", best.best), ("plain", {})):
+        r = renderer_for(sc, path, **over)
+        r.set_stream(stream.cuda_stream)
+        render_scene(r, sc)
+        ms = []
+        for _ in range(5):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            render_scene(r, sc)
+            b.record(stream)
+            torch.cuda.synchronize()
+            ms.append(a.elapsed_time(b))
+        st = r.stats()
+        m = statistics.median(ms)
+        out[path] = {"ms_per_frame": m, "value": st["micropolygons"] / (m / 1e3), "micropolygons": st["micropolygons"],
+                     "passes": st["passes"]}
+        r.close()
+    out["batched_over_plain"] = out["batched"]["value"] / out["plain"]["value"]
+    return out
 
 
 def main():
@@ -199,9 +241,12 @@ def main():
     from micropolis_gb300 import scenes
     from micropolis_gb300.renderer import Projection, renderer_for
 
+    from micropolis_gb300 import autotune
     sc = scenes.WORKLOADS[WORKLOAD]()
     stream = torch.cuda.Stream(dev)
-    r = renderer_for(sc, "batched")
+    # the autotuner times every knob setting on this frame and picks the fastest
+    tuned = autotune.tune(sc, frames=5, warmup=2, use_cache=False)
+    r = renderer_for(sc, "batched", **tuned.best)
     r.set_stream(stream.cuda_stream)
     proj = Projection(sc.fovy, sc.near, (sc.width, sc.height))
     handles = [1000 + k for k in range(len(sc.draws))]
@@ -294,6 +339,12 @@ def main():
     stage_ms = {k: statistics.median(v) for k, v in stage.items() if max(v) > 0}
     dominant = max(stage_ms, key=stage_ms.get)
 
+    # atomic roofline: fragments resolved by 64-bit atomicMin in the dice+raster
+    # stage against the device's measured atomicMin rate on a buffer of the
+    # key buffer's size (uniform random slots and 8x8-tile locality)
+    key_slots = ((W + 31) // 32 * 32) * ((H + 31) // 32 * 32)
+    atom_peak = {"random": r.atomic_bench(key_slots, 1 << 27, 0), "tiled": r.atomic_bench(key_slots, 1 << 27, 1)}
+
     peak_gbs, peak_kind = measured_peaks()
     n_cp_bytes = sum(d.mesh.n_patches * d.mesh.cp.shape[1] * 16 for d in sc.draws)
     S = stats["subpatches"]
@@ -307,9 +358,14 @@ def main():
     dom_bytes = alg.get(dominant, 0)
     dom_s = stage_ms[dominant] / 1e3
     achieved = dom_bytes / dom_s / 1e9 if dom_s > 0 else 0.0
+    raster_s = stage_ms.get("dice_raster", 0.0) / 1e3
+    atom_rate = frags / raster_s if raster_s > 0 else 0.0
     roofline = {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak_gbs, "unit": "GB/s",
-                "frac": achieved / peak_gbs, "traffic": None, "peak_kind": peak_kind,
-                "stage_ms": stage_ms, "alg_bytes": dom_bytes}
+                "frac": achieved / peak_gbs, "traffic": NCU_TRAFFIC.get(dominant), "peak_kind": peak_kind,
+                "stage_ms": stage_ms, "alg_bytes": dom_bytes,
+                "atomic": {"kernel": "dice_raster", "achieved": atom_rate, "peak": atom_peak["tiled"],
+                           "peak_random": atom_peak["random"], "unit": "atomicMin/s",
+                           "frac": atom_rate / atom_peak["tiled"] if atom_peak["tiled"] else None}}
 
     extras = {}
     if not args.no_extras and rank == 0:
@@ -349,10 +405,12 @@ def main():
             extras["adjoint"] = adjoint.bench_bwd_fwd(stream)
         except Exception as e:  # noqa: BLE001
             extras["adjoint"] = {"error": str(e)[:200]}
+        extras["views64"] = views64_leg(stream)
         # CPU baseline: bounded sample on the host cores
         cores = os.cpu_count() or 1
-        per = 96
-        cv, cmp, cwall, cbusy = cpu_baseline(WORKLOAD, cores, per)
+        per = 2048
+        with cpu_pool(cores) as pool:
+            cv, cmp, cwall, cbusy = cpu_baseline(WORKLOAD, cores, per, pool)
         extras["cpu_baseline"] = {"value": cv, "unit": "micropolygons/s", "cores": cores, "kind": "port",
                                   "sample": f"{cores} processes, each bound&split+dice+shade+sample of {per} of "
                                             f"the 4096 patches ({cmp} micropolygons in {cbusy:.1f} s)"}
@@ -369,6 +427,7 @@ def main():
                            "fragments_per_pixel": frags / (W * H),
                            "depth_complexity_covered": frags / max(covered, 1), "bounds": stats["bounds"],
                            "graph_ms_median": statistics.median(graph_ms),
+                           "tuned": tuned.best,
                            "wall_ms_per_frame": 1e3 * t_wall / args.steps},
                 "e2e": {"value": e2e_value, "unit": "micropolygons/s", "h2d_bytes_per_step": h2d,
                         "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * statistics.mean(e2e_times)},

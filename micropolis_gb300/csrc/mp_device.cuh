@@ -482,6 +482,7 @@ struct Tri {
     int Dx[3], Dy[3], O[3], C[3];
     int Px[3], Py[3];
     float dv[3];
+    float rdn;   // RN(1 / dn), dn = E_{e+1}(P_e), the same integer for e = 0, 1, 2
 };
 __device__ __forceinline__ int wmul(int a, int b) { return (int)((unsigned)a * (unsigned)b); }
 __device__ __forceinline__ int wadd(int a, int b) { return (int)((unsigned)a + (unsigned)b); }
@@ -503,6 +504,13 @@ __device__ __forceinline__ void tri_setup(Tri& t, int x0, int y0, float d0, int 
         t.O[e] = wadd(wmul(t.Dx[e], t.Px[e]), wmul(t.Dy[e], t.Py[e]));
         t.C[e] = (t.Dx[e] > 0 || (t.Dx[e] == 0 && t.Dy[e] > 0)) ? -1 : 0;
     }
+    // The barycentric denominator of kernels/reyes.cl:256-258 is edge e+1's
+    // function at vertex e.  With D = P_{e+1} - P_e and F = P_{e+2} - P_e it
+    // is D.y * F.x - D.x * F.y, minus twice the signed area, the same for all
+    // three e; wrapped int32 arithmetic is a ring, so the identity holds
+    // exactly and one reciprocal serves the three weights of every sample.
+    const int dn = wsub(wadd(wmul(t.Dx[1], t.Px[0]), wmul(t.Dy[1], t.Py[0])), t.O[1]);
+    t.rdn = frcp((float)dn);
 }
 
 // inside_triangle(): updates depth when the sample is inside and nearer.
@@ -514,11 +522,7 @@ __device__ __forceinline__ bool tri_test(const Tri& t, int tx, int ty, float& de
     if (ok) {
         float w[3];
 #pragma unroll
-        for (int e = 0; e < 3; ++e) {
-            int en = (e + 1) % 3;
-            int dn = wsub(wadd(wmul(t.Dx[en], t.Px[e]), wmul(t.Dy[en], t.Py[e])), t.O[en]);
-            w[e] = kdiv((float)V[en], (float)dn);
-        }
+        for (int e = 0; e < 3; ++e) w[e] = fmul((float)V[(e + 1) % 3], t.rdn);
         float d = ffma(t.dv[2], w[2], ffma(t.dv[1], w[1], fmul(t.dv[0], w[0])));
         if (d < depth) depth = d;
     }
@@ -527,7 +531,7 @@ __device__ __forceinline__ bool tri_test(const Tri& t, int tx, int ty, float& de
 
 // idepth = (int)(clamp(depth / 200, 0, 1) * 0x7fffffff) (kernels/reyes.cl:364)
 __device__ __forceinline__ unsigned idepth_of(float depth) {
-    float c = fminf(fmaxf(kdiv(depth, 200.0f), 0.0f), 1.0f);
+    float c = fminf(fmaxf(fmul(depth, 0.005f), 0.0f), 1.0f);   // 0.005f == RN(1 / 200)
     return (unsigned)__float2int_rz(fmul(c, 2147483648.0f));
 }
 

@@ -83,19 +83,33 @@ __device__ __forceinline__ bool quad_is_fast(const int* qx, const int* qy, int& 
     return (maxx - minx) <= kFastExtent && (maxy - miny) <= kFastExtent;
 }
 
+// A small quad whose two triangles both have the rejected winding covers
+// nothing (small quads: the products below cannot overflow).
+__device__ __forceinline__ bool quad_winding_ok(const int* qx, const int* qy) {
+    int d1x = qx[1] - qx[0], d1y = qy[1] - qy[0];
+    int d2x = qx[2] - qx[0], d2y = qy[2] - qy[0];
+    int d3x = qx[3] - qx[0], d3y = qy[3] - qy[0];
+    return d1x * d3y - d3x * d1y < 0 || d3x * d2y - d2x * d3y < 0;
+}
+// Pixels whose sample point lies in the fixed-point bbox, clipped to the
+// frame; false when there are none.
+__device__ __forceinline__ bool quad_pixels(const FrameDev& fr, int minx, int miny, int maxx, int maxy, int& x0,
+                                            int& y0, int& x1, int& y1) {
+    const int one = (1 << fr.shift) - 1;
+    x0 = max((minx + one) >> fr.shift, 0);
+    x1 = min(maxx >> fr.shift, fr.W - 1);
+    y0 = max((miny + one) >> fr.shift, 0);
+    y1 = min(maxy >> fr.shift, fr.H - 1);
+    return x0 <= x1 && y0 <= y1;
+}
+
 // Fast path: rasterize one quad over its own pixel bbox (see file header).
 __device__ __forceinline__ int raster_quad_fast(const FrameDev& fr, unsigned long long* keys, const int* qx,
                                                 const int* qy, const float* qd, int minx, int miny, int maxx,
                                                 int maxy, unsigned mp_id) {
-    // a quad whose two triangles both have the rejected winding covers nothing
-    int d1x = qx[1] - qx[0], d1y = qy[1] - qy[0];
-    int d2x = qx[2] - qx[0], d2y = qy[2] - qy[0];
-    int d3x = qx[3] - qx[0], d3y = qy[3] - qy[0];
-    if (!(d1x * d3y - d3x * d1y < 0 || d3x * d2y - d2x * d3y < 0)) return 0;
-    const int one = (1 << fr.shift) - 1;
-    int x0 = max((minx + one) >> fr.shift, 0), x1 = min(maxx >> fr.shift, fr.W - 1);
-    int y0 = max((miny + one) >> fr.shift, 0), y1 = min(maxy >> fr.shift, fr.H - 1);
-    if (x0 > x1 || y0 > y1) return 0;
+    if (!quad_winding_ok(qx, qy)) return 0;
+    int x0, y0, x1, y1;
+    if (!quad_pixels(fr, minx, miny, maxx, maxy, x0, y0, x1, y1)) return 0;
     Tri t1, t2;
     tri_setup(t1, qx[0], qy[0], qd[0], qx[1], qy[1], qd[1], qx[3], qy[3], qd[3]);
     tri_setup(t2, qx[0], qy[0], qd[0], qx[3], qy[3], qd[3], qx[2], qy[2], qd[2]);
@@ -154,6 +168,8 @@ struct FusedSmem {
     int bound[NS][NB][4];
     int tiles[NS][NB][4];     // block tile range; tiles[k][b][0] > tiles[k][b][2] marks a skipped block
     unsigned zero[NS];
+    unsigned n_live;
+    unsigned short live[NS * PS * PS];   // quads that may touch a pixel, in bound-phase order
     float tx[NS][G], ty[NS][G];
     float4 vw[NS][G], cw[NS][G];
     int px[NS * NV], py[NS * NV];
@@ -177,6 +193,7 @@ __device__ __forceinline__ void raster_group(FusedSmem<PS, NS>& sm, long long ba
         sm.meta[tid] = sub.meta[base + tid];
         sm.zero[tid] = 0;
     }
+    if (tid == 0) sm.n_live = 0;
     for (int i = tid; i < n * NB; i += kFusedThreads) {
         int* b = sm.bound[i / NB][i % NB];
         b[0] = vmaxx; b[1] = vmaxy; b[2] = 0; b[3] = 0;
@@ -233,13 +250,25 @@ __device__ __forceinline__ void raster_group(FusedSmem<PS, NS>& sm, long long ba
         }
     }
     __syncthreads();
-    // block bounds over front-facing quads (kernels/reyes.cl:120-166)
+    // block bounds over front-facing quads (kernels/reyes.cl:120-166), and
+    // the list of quads that can touch a pixel: a quad with a large bbox, or
+    // a small one with an accepted winding and a pixel centre in its bbox
     for (int i = tid; i < n * NQ; i += kFusedThreads) {
         const int k = i / NQ, q = i % NQ;
         const int nu = q % PS, nv = q / PS, i0 = k * NV + nu + nv * G;
         const int qx[4] = {sm.px[i0], sm.px[i0 + 1], sm.px[i0 + G], sm.px[i0 + G + 1]};
         const int qy[4] = {sm.py[i0], sm.py[i0 + 1], sm.py[i0 + G], sm.py[i0 + G + 1]};
         QuadBound qb = quad_block_bound(fr, qx, qy);
+        {
+            int minx, miny, maxx, maxy, x0, y0, x1, y1;
+            const bool live = !quad_is_fast(qx, qy, minx, miny, maxx, maxy) ||
+                              (quad_winding_ok(qx, qy) && quad_pixels(fr, minx, miny, maxx, maxy, x0, y0, x1, y1));
+            const unsigned lm = __ballot_sync(0xffffffffu, live);
+            unsigned at = 0;
+            if ((tid & 31) == 0 && lm) at = atomicAdd(&sm.n_live, (unsigned)__popc(lm));
+            at = __shfl_sync(0xffffffffu, at, 0);
+            if (live) sm.live[at + __popc(lm & lanemask_lt())] = (unsigned short)i;
+        }
         if (!qb.ff) { qb.pminx = vmaxx; qb.pminy = vmaxy; qb.pmaxx = 0; qb.pmaxy = 0; }
         // lanes of one (sub-patch, block) reduce in registers, then one
         // shared atomic per group (n * NQ is a multiple of 32: whole warps)
@@ -266,8 +295,10 @@ __device__ __forceinline__ void raster_group(FusedSmem<PS, NS>& sm, long long ba
         }
     }
     __syncthreads();
-    // rasterize every quad of a live block
-    for (int i = tid; i < n * NQ; i += kFusedThreads) {
+    // rasterize the listed quads of live blocks
+    const int n_live = (int)sm.n_live;
+    for (int j = tid; j < n_live; j += kFusedThreads) {
+        const int i = sm.live[j];
         const int k = i / NQ, q = i % NQ;
         const int nu = q % PS, nv = q / PS, blk = (nu >> 3) + (nv >> 3) * BPL;
         const int* tp = sm.tiles[k][blk];
