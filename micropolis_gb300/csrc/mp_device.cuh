@@ -123,7 +123,9 @@ __device__ __forceinline__ F3 blend3(float a, const F3& A, float b, const F3& B,
     return F3{fdiv(fadd(fmul(a, A.x), fmul(b, B.x)), den), fdiv(fadd(fmul(a, A.y), fmul(b, B.y)), den),
               fdiv(fadd(fmul(a, A.z), fmul(b, B.z)), den)};
 }
-__device__ __forceinline__ F3 eval_gregory_cpu(const float4* pd, float u_in, float v_in) {
+// Not inlined: the nine calls of bound_range share one copy of the code,
+// which keeps the bound-and-split loop inside the instruction cache.
+static __device__ __noinline__ F3 eval_gregory_cpu(const float4* pd, float u_in, float v_in) {
     float u = v_in, v = u_in;  // std::swap(u, v)
     F3 F0 = blend3(u, ld3(pd + 12), v, ld3(pd + 16), fadd(u, v));
     F3 F1 = blend3(fsub(1.0f, u), ld3(pd + 17), v, ld3(pd + 13), fadd(fsub(1.0f, u), v));
@@ -158,19 +160,17 @@ __device__ __forceinline__ void bbox_add(RangeBound& b, const F3& p) {
     b.bmax.z = maximum(p.z, b.bmax.z);
 }
 
-// The 9 samples are visited column by column (iv outer, iu inner) so that
-// only one column and the previous one are live.  Every value is formed by
+// The 9 samples are visited column by column (iv outer, iu inner, the
+// column loop not unrolled) so that only one column and the previous one are
+// live and the code stays small.  Every value is formed by
 // the reference's operations in the reference's order: the column sum v_iv is
 // (0 + d01) + d12, the row sums h_iu accumulate across columns in the same
 // order, vlen/hlen take maximum() in index order 0, 1, 2, and the bbox
 // (minimum/maximum that skip NaN) does not depend on the visiting order.
 __device__ __forceinline__ RangeBound bound_range(const DrawDev& d, int pid, float4 r) {
-    float sv[3], su[3];
+    float sv[3];
 #pragma unroll
-    for (int i = 0; i < 3; ++i) {
-        sv[i] = fadd(r.x, fmul(fmul(fsub(r.z, r.x), (float)i), 0.5f));
-        su[i] = fadd(r.y, fmul(fmul(fsub(r.w, r.y), (float)i), 0.5f));
-    }
+    for (int i = 0; i < 3; ++i) sv[i] = fadd(r.x, fmul(fmul(fsub(r.z, r.x), (float)i), 0.5f));
     RangeBound b;
     const float inf = __int_as_float(0x7f800000);
     b.bmin = F3{inf, inf, inf};
@@ -178,13 +178,14 @@ __device__ __forceinline__ RangeBound bound_range(const DrawDev& d, int pid, flo
     b.vlen = 0.0f;
     float hsum[3] = {0.0f, 0.0f, 0.0f};
     F3 prev[3];
-#pragma unroll
+#pragma unroll 1
     for (int iv = 0; iv < 3; ++iv) {
         F3 cur[3];
+        const float su_iv = fadd(r.y, fmul(fmul(fsub(r.w, r.y), (float)iv), 0.5f));
         if (d.type == 0) {
             // eval_patch(P, t = u, s = v): rows P[i][0..3] in t, then the column in s
             const float4* P = d.cp + (size_t)pid * 16;
-            SplineW wt = spline_weights(su[iv]);
+            SplineW wt = spline_weights(su_iv);
             F3 row[4];
 #pragma unroll
             for (int i = 0; i < 4; ++i)
@@ -195,7 +196,7 @@ __device__ __forceinline__ RangeBound bound_range(const DrawDev& d, int pid, flo
         } else {
             const float4* P = d.cp + (size_t)pid * 20;
 #pragma unroll
-            for (int iu = 0; iu < 3; ++iu) cur[iu] = mv_point(d.mv, eval_gregory_cpu(P, su[iv], sv[iu]));
+            for (int iu = 0; iu < 3; ++iu) cur[iu] = mv_point(d.mv, eval_gregory_cpu(P, su_iv, sv[iu]));
         }
 #pragma unroll
         for (int iu = 0; iu < 3; ++iu) bbox_add(b, cur[iu]);

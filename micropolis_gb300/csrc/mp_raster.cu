@@ -153,18 +153,29 @@ __device__ __forceinline__ void push_big(BigQuad* big, long long big_cap, unsign
 
 // The fused kernel works on groups of NS sub-patches per 256-thread block:
 // NS * (PS+1)^2 dice vertices are spread over all threads (22 * 81 = 1782 =
-// 7 rounds of 256 at PS = 8), then the block bounds, then one thread per quad.
+// 7 rounds of 256 at PS = 8), then the block bounds, then one thread per quad
+// that can touch a pixel.  The inputs of the next group (sub-patch records,
+// control points, matrices) are copied into the other half of a double
+// buffer with cp.async while the current group is diced and rasterized.
 constexpr int kFusedThreads = 256;
+
+static_assert(offsetof(DrawDev, proj) == offsetof(DrawDev, mv) + 16 * sizeof(float), "mv, proj adjacent");
+static_assert(offsetof(DrawDev, mv) % 16 == 0 && sizeof(DrawDev) % 16 == 0, "16-byte copies of mv/proj");
+
+// Inputs of one group.
+template <int NS>
+struct GroupStage {
+    float4 cp[NS][20];
+    float mvp[NS][32];        // modelview, then projection
+    float4 range[NS];
+    int2 meta[NS];            // (patch id, draw)
+    int tv[NS][2];            // draw type, view
+};
 
 template <int PS, int NS_>
 struct FusedSmem {
     static constexpr int NS = NS_, G = PS + 1, NV = G * G, NB = (PS / 8) * (PS / 8);
-    float4 cp[NS][20];
-    float mv[NS][16];
-    float proj[NS][16];
-    float4 range[NS];
-    int2 meta[NS];
-    int type[NS], view[NS];
+    GroupStage<NS> st[2];
     int bound[NS][NB][4];
     int tiles[NS][NB][4];     // block tile range; tiles[k][b][0] > tiles[k][b][2] marks a skipped block
     unsigned zero[NS];
@@ -177,44 +188,90 @@ struct FusedSmem {
     float ex[NS * NV], ey[NS * NV], ez[NS * NV];
 };
 
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    const size_t ga = __cvta_generic_to_global(gmem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(sa), "l"(ga) : "memory");
+}
+__device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    const size_t ga = __cvta_generic_to_global(gmem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(sa), "l"(ga) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+// Copies, for the n sub-patches whose records are already in st.meta, their
+// control points, matrices, type and view (asynchronous; the caller waits).
+template <int NS>
+__device__ __forceinline__ void stage_inputs(GroupStage<NS>& st, int n, const DrawDev* __restrict__ draws) {
+    for (int i = threadIdx.x; i < n * 32; i += kFusedThreads) {
+        const int k = i >> 5, c = i & 31;
+        const int2 m = st.meta[k];
+        const DrawDev* d = draws + m.y;
+        if (c < 20) {
+            const int ncp = d->type == 0 ? 16 : 20;
+            if (c < ncp) cp_async16(&st.cp[k][c], d->cp + (size_t)m.x * ncp + c);
+        } else if (c < 28) {
+            cp_async16(&st.mvp[k][4 * (c - 20)], d->mv + 4 * (c - 20));
+        } else if (c == 28) {
+            cp_async4(&st.tv[k][0], &d->type);
+        } else if (c == 29) {
+            cp_async4(&st.tv[k][1], &d->view);
+        }
+    }
+    cp_async_commit();
+}
+
+// Stages the group [base, base + n) into st from scratch (records, then
+// inputs) and waits for it; ends with a barrier.
+template <int NS>
+__device__ __forceinline__ void stage_group(GroupStage<NS>& st, long long base, int n, const SubPatches& sub,
+                                            const DrawDev* __restrict__ draws) {
+    if ((int)threadIdx.x < n) {
+        st.range[threadIdx.x] = sub.range[base + threadIdx.x];
+        st.meta[threadIdx.x] = sub.meta[base + threadIdx.x];
+    }
+    __syncthreads();
+    stage_inputs(st, n, draws);
+    cp_async_wait_all();
+    __syncthreads();
+}
+
 // Dices, shades and rasterizes the n (<= NS) sub-patches at [base, base+n)
-// of the emitted list with the whole block; ends with a barrier.
+// of the emitted list, whose inputs are staged in sm.st[b], with the whole
+// block; meanwhile stages the n_next sub-patches at next_base into
+// sm.st[b ^ 1].  Ends with a barrier after which both are complete.
 template <int PS, int NS>
-__device__ __forceinline__ void raster_group(FusedSmem<PS, NS>& sm, long long base, int n, const DrawDev* __restrict__ draws,
+__device__ __forceinline__ void raster_group(FusedSmem<PS, NS>& sm, int b, long long base, int n,
+                                             long long next_base, int n_next, const DrawDev* __restrict__ draws,
                                              const FrameDev& fr, const SubPatches& sub, const Framebuffer& fb,
                                              float* __restrict__ mshade, BigQuad* big, long long big_cap,
                                              unsigned long long* ctrl, const V3& light, long long& frags) {
     using SM = FusedSmem<PS, NS>;
     constexpr int G = SM::G, NV = SM::NV, NQ = PS * PS, BPL = PS / 8, NB = SM::NB;
-    const int tid = threadIdx.x;
+    GroupStage<NS>& cur = sm.st[b];
+    GroupStage<NS>& nxt = sm.st[b ^ 1];
+    const int tid = threadIdx.x, lane = tid & 31;
     const int vmaxx = (fr.W << fr.shift) - 1, vmaxy = (fr.H << fr.shift) - 1;
-    if (tid < n) {
-        sm.range[tid] = sub.range[base + tid];
-        sm.meta[tid] = sub.meta[base + tid];
-        sm.zero[tid] = 0;
+    // the next group's records travel in registers until this group's
+    // vertices are done
+    float4 next_range = make_float4(0.f, 0.f, 0.f, 0.f);
+    int2 next_meta = make_int2(0, 0);
+    if (tid < n_next) {
+        next_range = sub.range[next_base + tid];
+        next_meta = sub.meta[next_base + tid];
     }
+    if (tid < n) sm.zero[tid] = 0;
     if (tid == 0) sm.n_live = 0;
     for (int i = tid; i < n * NB; i += kFusedThreads) {
-        int* b = sm.bound[i / NB][i % NB];
-        b[0] = vmaxx; b[1] = vmaxy; b[2] = 0; b[3] = 0;
-    }
-    __syncthreads();
-    for (int i = tid; i < n * 20; i += kFusedThreads) {
-        const int k = i / 20, c = i % 20;
-        const DrawDev& d = draws[sm.meta[k].y];
-        const int ncp = d.type == 0 ? 16 : 20;
-        if (c < ncp) sm.cp[k][c] = __ldg(d.cp + (size_t)sm.meta[k].x * ncp + c);
-    }
-    for (int i = tid; i < n * 32; i += kFusedThreads) {
-        const int k = i >> 5, c = i & 31;
-        const DrawDev& d = draws[sm.meta[k].y];
-        if (c < 16) sm.mv[k][c] = d.mv[c]; else sm.proj[k][c - 16] = d.proj[c - 16];
-        if (c == 0) { sm.type[k] = d.type; sm.view[k] = d.view; }
+        int* bb = sm.bound[i / NB][i % NB];
+        bb[0] = vmaxx; bb[1] = vmaxy; bb[2] = 0; bb[3] = 0;
     }
     // dice parameters and Bernstein weights of each row / column of vertices
     for (int i = tid; i < n * 2 * G; i += kFusedThreads) {
         const int k = i / (2 * G), c = i % (2 * G);
-        const float4 rg = sm.range[k];
+        const float4 rg = cur.range[k];
         if (c < G) {
             const float t = dice_param(rg.x, rg.z, c, fr);
             sm.tx[k][c] = t;
@@ -230,11 +287,12 @@ __device__ __forceinline__ void raster_group(FusedSmem<PS, NS>& sm, long long ba
     for (int i = tid; i < n * NV; i += kFusedThreads) {
         const int k = i / NV, v = i % NV;
         const int nu = v % G, nv = v / G;
-        float4 pos = dice_eye_w(sm.type[k], sm.mv[k], fr, sm.cp[k], sm.tx[k][nu], sm.ty[k][nv], sm.vw[k][nu],
+        const float* mvp = cur.mvp[k];
+        float4 pos = dice_eye_w(cur.tv[k][0], mvp, fr, cur.cp[k], sm.tx[k][nu], sm.ty[k][nv], sm.vw[k][nu],
                                 sm.cw[k][nv]);
         int px, py;
         float dep;
-        project_vertex_m(sm.proj[k], fr, pos, px, py, dep);
+        project_vertex_m(mvp + 16, fr, pos, px, py, dep);
         sm.px[i] = px;
         sm.py[i] = py;
         sm.dep[i] = dep;
@@ -249,47 +307,63 @@ __device__ __forceinline__ void raster_group(FusedSmem<PS, NS>& sm, long long ba
             atomicOr(&sm.zero[k], zb);
         }
     }
+    if (tid < n_next) {
+        nxt.range[tid] = next_range;
+        nxt.meta[tid] = next_meta;
+    }
     __syncthreads();
-    // block bounds over front-facing quads (kernels/reyes.cl:120-166), and
+    if (n_next > 0) stage_inputs(nxt, n_next, draws);
+    // Block bounds over front-facing quads (kernels/reyes.cl:120-166), and
     // the list of quads that can touch a pixel: a quad with a large bbox, or
-    // a small one with an accepted winding and a pixel centre in its bbox
+    // a small one with an accepted winding and a pixel centre in its bbox.
+    // n * NQ is a multiple of 32, so whole warps run each round; the quads of
+    // one warp share a sub-patch, and their 8x8 blocks are fixed by the lane:
+    // one block at PS = 8, and at PS = 16 two, lanes with bit 3 clear / set.
     for (int i = tid; i < n * NQ; i += kFusedThreads) {
         const int k = i / NQ, q = i % NQ;
         const int nu = q % PS, nv = q / PS, i0 = k * NV + nu + nv * G;
         const int qx[4] = {sm.px[i0], sm.px[i0 + 1], sm.px[i0 + G], sm.px[i0 + G + 1]};
         const int qy[4] = {sm.py[i0], sm.py[i0 + 1], sm.py[i0 + G], sm.py[i0 + G + 1]};
-        QuadBound qb = quad_block_bound(fr, qx, qy);
-        {
-            int minx, miny, maxx, maxy, x0, y0, x1, y1;
-            const bool live = !quad_is_fast(qx, qy, minx, miny, maxx, maxy) ||
-                              (quad_winding_ok(qx, qy) && quad_pixels(fr, minx, miny, maxx, maxy, x0, y0, x1, y1));
-            const unsigned lm = __ballot_sync(0xffffffffu, live);
-            unsigned at = 0;
-            if ((tid & 31) == 0 && lm) at = atomicAdd(&sm.n_live, (unsigned)__popc(lm));
-            at = __shfl_sync(0xffffffffu, at, 0);
-            if (live) sm.live[at + __popc(lm & lanemask_lt())] = (unsigned short)i;
-        }
-        if (!qb.ff) { qb.pminx = vmaxx; qb.pminy = vmaxy; qb.pmaxx = 0; qb.pmaxy = 0; }
-        // lanes of one (sub-patch, block) reduce in registers, then one
-        // shared atomic per group (n * NQ is a multiple of 32: whole warps)
-        const unsigned grp = __match_any_sync(0xffffffffu, k * NB + (nu >> 3) + (nv >> 3) * BPL);
-        const int x0 = __reduce_min_sync(grp, qb.pminx), y0 = __reduce_min_sync(grp, qb.pminy);
-        const int x1 = __reduce_max_sync(grp, qb.pmaxx), y1 = __reduce_max_sync(grp, qb.pmaxy);
-        if ((tid & 31) == __ffs(grp) - 1) {
-            int* b = sm.bound[k][(nu >> 3) + (nv >> 3) * BPL];
-            atomicMin(b + 0, x0);
-            atomicMin(b + 1, y0);
-            atomicMax(b + 2, x1);
-            atomicMax(b + 3, y1);
+        const int minx = min(min(qx[0], qx[1]), min(qx[2], qx[3]));
+        const int maxx = max(max(qx[0], qx[1]), max(qx[2], qx[3]));
+        const int miny = min(min(qy[0], qy[1]), min(qy[2], qy[3]));
+        const int maxy = max(max(qy[0], qy[1]), max(qy[2], qy[3]));
+        // is_front_facing (kernels/reyes.cl:54-65) on wrapped int32
+        const int d1x = wsub(qx[1], qx[0]), d1y = wsub(qy[1], qy[0]);
+        const int d2x = wsub(qx[2], qx[0]), d2y = wsub(qy[2], qy[0]);
+        const int d3x = wsub(qx[3], qx[0]), d3y = wsub(qy[3], qy[0]);
+        const bool wind = wsub(wmul(d1x, d3y), wmul(d3x, d1y)) < 0 || wsub(wmul(d3x, d2y), wmul(d2x, d3y)) < 0;
+        const bool fast = minx >= -kFastCoord && maxx <= kFastCoord && miny >= -kFastCoord && maxy <= kFastCoord &&
+                          maxx - minx <= kFastExtent && maxy - miny <= kFastExtent;
+        int x0, y0, x1, y1;
+        const bool live = !fast || (wind && quad_pixels(fr, minx, miny, maxx, maxy, x0, y0, x1, y1));
+        const unsigned lm = __ballot_sync(0xffffffffu, live);
+        unsigned at = 0;
+        if (lane == 0 && lm) at = atomicAdd(&sm.n_live, (unsigned)__popc(lm));
+        at = __shfl_sync(0xffffffffu, at, 0);
+        if (live) sm.live[at + __popc(lm & lanemask_lt())] = (unsigned short)i;
+        // the block bound starts at (viewport max, 0) and takes front-facing quads
+        const bool ff = !fr.backface || wind;
+        const unsigned grp = PS == 8 ? 0xffffffffu : ((lane & 8) ? 0xff00ff00u : 0x00ff00ffu);
+        const int bx0 = __reduce_min_sync(grp, ff ? min(vmaxx, minx) : vmaxx);
+        const int by0 = __reduce_min_sync(grp, ff ? min(vmaxy, miny) : vmaxy);
+        const int bx1 = __reduce_max_sync(grp, ff ? max(0, maxx) : 0);
+        const int by1 = __reduce_max_sync(grp, ff ? max(0, maxy) : 0);
+        if ((lane & (PS == 8 ? 31 : 23)) == 0) {
+            int* bb = sm.bound[k][(nu >> 3) + (nv >> 3) * BPL];
+            atomicMin(bb + 0, bx0);
+            atomicMin(bb + 1, by0);
+            atomicMax(bb + 2, bx1);
+            atomicMax(bb + 3, by1);
         }
     }
     __syncthreads();
     // the tile range of each block, or a skip mark
     for (int i = tid; i < n * NB; i += kFusedThreads) {
-        const int k = i / NB, b = i % NB;
-        const int* bb = sm.bound[k][b];
-        int* t = sm.tiles[k][b];
-        if (!block_tiles(fr, bb[0], bb[1], bb[2], bb[3], !((sm.zero[k] >> b) & 1), t)) {
+        const int k = i / NB, bk = i % NB;
+        const int* bb = sm.bound[k][bk];
+        int* t = sm.tiles[k][bk];
+        if (!block_tiles(fr, bb[0], bb[1], bb[2], bb[3], !((sm.zero[k] >> bk) & 1), t)) {
             t[0] = 1;
             t[2] = 0;
         }
@@ -316,7 +390,7 @@ __device__ __forceinline__ void raster_group(FusedSmem<PS, NS>& sm, long long ba
         }
         const long long s = base + k;
         const unsigned mp_id = (unsigned)(s * NQ + nu + nv * PS);
-        const int view = sm.view[k];
+        const int view = cur.tv[k][1];
         unsigned long long* keys = fb.keys + (long long)view * fb.key_pixels;
         int minx, miny, maxx, maxy, f = 0;
         const bool fast = quad_is_fast(qx, qy, minx, miny, maxx, maxy);
@@ -333,6 +407,7 @@ __device__ __forceinline__ void raster_group(FusedSmem<PS, NS>& sm, long long ba
         }
         frags += f;
     }
+    cp_async_wait_all();
     __syncthreads();
 }
 
@@ -347,9 +422,15 @@ __global__ void __launch_bounds__(kFusedThreads, 3)
     if (S > sub.capacity) S = sub.capacity;
     const V3 light = light_dir();
     long long frags = 0;
-    for (long long base = (long long)blockIdx.x * NS; base < S; base += (long long)gridDim.x * NS)
-        raster_group<PS, NS>(sm, base, (int)min((long long)NS, S - base), draws, fr, sub, fb, mshade, big, big_cap,
-                             ctrl, light, frags);
+    const long long stride = (long long)gridDim.x * NS;
+    long long base = (long long)blockIdx.x * NS;
+    if (base < S) stage_group(sm.st[0], base, (int)min((long long)NS, S - base), sub, draws);
+    for (int b = 0; base < S; base += stride, b ^= 1) {
+        const long long next = base + stride;
+        raster_group<PS, NS>(sm, b, base, (int)min((long long)NS, S - base), next,
+                             next < S ? (int)min((long long)NS, S - next) : 0, draws, fr, sub, fb, mshade, big,
+                             big_cap, ctrl, light, frags);
+    }
     frags = __reduce_add_sync(0xffffffffu, (unsigned)frags);
     if ((threadIdx.x & 31) == 0 && frags) atomicAdd(cw(ctrl, kFragments), (unsigned long long)frags);
 }
@@ -418,7 +499,8 @@ __global__ void __launch_bounds__(kFusedThreads, 3)
         }
         const int n = __syncthreads_count(ready);
         if (n == 0 || __syncthreads_or(gave_up)) break;
-        raster_group<PS, NS>(sm, base, n, gdraws, fr, sub, fb, mshade, big, big_cap, ctrl, light, frags);
+        stage_group(sm.st[0], base, n, sub, gdraws);
+        raster_group<PS, NS>(sm, 0, base, n, 0, 0, gdraws, fr, sub, fb, mshade, big, big_cap, ctrl, light, frags);
     }
     frags = __reduce_add_sync(0xffffffffu, (unsigned)frags);
     if ((threadIdx.x & 31) == 0 && frags) atomicAdd(cw(ctrl, kFragments), (unsigned long long)frags);
