@@ -110,16 +110,24 @@ class Result:
     cached: bool = False
 
 
-def choose(trials: List[Trial], by_rate: bool) -> Trial:
+MARGIN = 0.01
+
+
+def choose(trials: List[Trial], by_rate: bool, margin: float = MARGIN) -> Trial:
     """Lowest frame time, or highest micropolygon rate when the dice grid is
-    among the knobs.  Ties keep the earlier (default-first) candidate."""
+    among the knobs.  Among the trials within `margin` (relative) of the best
+    score, the earliest candidate wins: the search space lists the defaults
+    and the simpler settings first, and the choice does not flip between runs
+    on differences below the timing noise."""
     if not trials:
         raise ValueError("no trials")
-    best = trials[0]
-    for t in trials[1:]:
-        if (t.mpps > best.mpps) if by_rate else (t.ms < best.ms):
-            best = t
-    return best
+    score = [(t.mpps if by_rate else -t.ms) for t in trials]
+    top = max(score)
+    tol = abs(top) * margin
+    for t, v in zip(trials, score):
+        if v >= top - tol:
+            return t
+    return trials[0]
 
 
 def load_cache(path: Optional[str] = None) -> dict:

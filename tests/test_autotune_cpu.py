@@ -27,6 +27,10 @@ def test_choose_by_time_and_by_rate():
          autotune.Trial({"a": 2}, 1.5, 100), autotune.Trial({"a": 3}, 3.0, 400)]
     assert autotune.choose(t, by_rate=False).options == {"a": 1}      # ties keep the earlier one
     assert autotune.choose(t, by_rate=True).options == {"a": 3}
+    # within the margin the earlier candidate wins
+    near = [autotune.Trial({"a": 0}, 1.005, 100), autotune.Trial({"a": 1}, 1.0, 100)]
+    assert autotune.choose(near, by_rate=False).options == {"a": 0}
+    assert autotune.choose(near, by_rate=False, margin=0.0).options == {"a": 1}
     with pytest.raises(ValueError):
         autotune.choose([], by_rate=False)
 
