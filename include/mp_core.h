@@ -97,6 +97,7 @@ typedef struct {
      * (plain: dice), 3 exact slow raster, 4 resolve (plain: shade), 5 plain sample,
      * 6 plain pass resolve, 7 plain host readback gaps */
     double stage_ms[8];
+    int64_t kernels;                /* kernel launches of the last frame (graph nodes included) */
 } mp_stats;
 
 typedef struct mp_ctx mp_ctx;

@@ -39,7 +39,7 @@ class MpProjection(ctypes.Structure):
 class MpStats(ctypes.Structure):
     _fields_ = [("subpatches", ctypes.c_int64), ("micropolygons", ctypes.c_int64), ("bounds", ctypes.c_int64),
                 ("passes", ctypes.c_int64), ("fragments", ctypes.c_int64), ("big_quads", ctypes.c_int64),
-                ("gpu_ms", ctypes.c_double), ("stage_ms", ctypes.c_double * 8)]
+                ("gpu_ms", ctypes.c_double), ("stage_ms", ctypes.c_double * 8), ("kernels", ctypes.c_int64)]
 
 
 c_void_p = ctypes.c_void_p

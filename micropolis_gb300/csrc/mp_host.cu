@@ -95,7 +95,7 @@ struct mp_ctx {
     size_t staging_bytes = 0;
     cudaEvent_t sev[8] = {};
     mp_stats stats{};
-    long long plain_bounds = 0, plain_passes = 0, plain_out = 0;
+    long long plain_bounds = 0, plain_passes = 0, plain_out = 0, plain_kernels = 0;
 };
 
 namespace {
@@ -305,6 +305,7 @@ mp_status plain_draw(mp_ctx* c, int draw_index) {
     mp_status st = ensure_plain(c, (long long)d.n_patches + 2 * P * (c->opt.max_split_depth + 2));
     if (st) return st;
     launch_bns_init_stack(c->stack, draw_index, d.n_patches, c->stream);
+    c->plain_kernels += 1;
     long long h = d.n_patches;
     while (h > 0) {
         long long b = std::min(h, P);
@@ -321,6 +322,7 @@ mp_status plain_draw(mp_ctx* c, int draw_index) {
         launch_bns_pass(c->d_draws, c->fr, c->stack, h, (int)b, c->pad_range, c->pad_meta, c->dec, c->keys,
                         c->scan_state, c->sub, c->plain_out, c->ctrl, c->opt.spin_limit, c->stream);
         CK(cudaGetLastError());
+        c->plain_kernels += 3;   // bound, scan, move
         if (c->stage_timing) CK(cudaEventRecord(c->sev[1], c->stream));
         st = read_ctrl(c);
         if (c->stage_timing) {
@@ -352,6 +354,7 @@ mp_status plain_draw(mp_ctx* c, int draw_index) {
             CK(cudaMemsetAsync(c->ctrl + kBigCount * kCtrlStride, 0, sizeof(unsigned long long), c->stream));
             if (tm) CK(cudaEventRecord(c->sev[6], c->stream));
             launch_pass_resolve(c->fr, c->fb, c->plain_out, n, c->color_grid, c->stream);
+            c->plain_kernels += 5;   // dice, shade, sample, exact slow raster, pass resolve
             if (tm) CK(cudaEventRecord(c->sev[7], c->stream));
             CK(cudaGetLastError());
             if (tm) {
@@ -814,11 +817,13 @@ mp_status mp_prepare(mp_ctx* c) {
     c->frame_valid = false;
     c->draws.clear();
     c->plain_bounds = c->plain_passes = c->plain_out = 0;
+    c->plain_kernels = 0;
     for (double& v : c->stats.stage_ms) v = 0;
     if (c->opt.path == MP_PATH_PLAIN) {
         CK(cudaEventRecord(c->ev0, c->stream));
         launch_bns_reset(c->ctrl, 0, c->stream);
         launch_clear(c->fb, c->fr, 1, c->stream);
+        c->plain_kernels += 2;
         CK(cudaGetLastError());
     }
     return MP_OK;
@@ -859,6 +864,8 @@ mp_status mp_finish(mp_ctx* c) {
         c->stats.subpatches = std::min((long long)hc(c, kOutCount), c->sub.capacity);
         c->stats.bounds = (long long)(hc(c, kQTail) >> 32);
         c->stats.passes = 1;
+        // reset, clear, (bound-and-split, dice+raster | one overlapped kernel), exact slow raster, resolve
+        c->stats.kernels = c->opt.overlap ? 5 : 6;
     } else {
         CK(cudaEventRecord(c->ev1, c->stream));
         st = read_ctrl(c);
@@ -867,6 +874,7 @@ mp_status mp_finish(mp_ctx* c) {
         c->stats.subpatches = c->plain_out;
         c->stats.bounds = c->plain_bounds;
         c->stats.passes = c->plain_passes;
+        c->stats.kernels = c->plain_kernels;
         if (c->stage_timing) {
             float ms = 0;
             cudaEventElapsedTime(&ms, c->ev0, c->ev1);
