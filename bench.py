@@ -37,10 +37,12 @@ L2_FLUSH_BYTES = 256 << 20
 
 # DRAM bytes (read + write) per launch of each stage's kernel on this
 # workload, from one ncu capture each (dram__bytes_read.sum +
-# dram__bytes_write.sum; profiles/raster_fused_mixed4096_1920x1080.md and
-# profiles/bns_persistent_mixed4096_1920x1080.md).  ncu replays with cold
+# dram__bytes_write.sum; profiles/raster_fused_mixed4096_1920x1080.md,
+# profiles/bns_persistent_mixed4096_1920x1080.md and
+# profiles/resolve_mixed4096_1920x1080.md).  ncu replays with cold
 # caches, so these are upper bounds for a launch inside a frame.
-NCU_TRAFFIC = {"dice_raster": 102_550_272 + 66_520_320, "bound_split": 2_525_184 + 26_926_080}
+NCU_TRAFFIC = {"dice_raster": 102_631_936 + 65_886_976, "bound_split": 2_533_120 + 27_202_816,
+               "resolve_or_shade": 62_764_032 + 8_419_328}
 
 
 def parse():
