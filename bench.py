@@ -52,6 +52,9 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-extras", action="store_true", help="skip plain/adjoint/cpu legs")
+    ap.add_argument("--all-configs", action="store_true",
+                    help="one line per workload (batched, plain, CPU oracle, backward/forward) instead of the bench line")
+    ap.add_argument("--workload", action="append", help="with --all-configs: only these workloads")
     ap.add_argument("--no-tune", action="store_true",
                     help="render with the default knob values instead of the autotuner's choice (profiling runs)")
     return ap.parse_args()
@@ -137,17 +140,23 @@ def _cpu_chunk(args):
 
 def cpu_baseline(name: str, procs: int, patches_per_proc: int, pool=None):
     """micropolygons/s of the oracle path on `procs` processes, each rendering
-    its own slice of every draw's patches (a bounded sample).  Returns
-    (rate, micropolygons, wall s, busiest process s)."""
+    its own slice of every draw's patches (a bounded sample); with
+    patches_per_proc = 0 the processes share one frame (process p renders the
+    p-th of `procs` equal parts of every draw).  Returns (rate,
+    micropolygons, wall s, busiest process s)."""
     from micropolis_gb300 import scenes
     sc = scenes.WORKLOADS[name]()
     jobs = []
     for p in range(procs):
         sl = []
         for d in sc.draws:
+            n = d.mesh.n_patches
+            if patches_per_proc <= 0:
+                sl.append((n * p // procs, n * (p + 1) // procs))
+                continue
             share = max(1, patches_per_proc // len(sc.draws))
-            a = (p * share) % max(1, d.mesh.n_patches)
-            sl.append((a, min(a + share, d.mesh.n_patches)))
+            a = (p * share) % max(1, n)
+            sl.append((a, min(a + share, n)))
         jobs.append((name, sl))
     t = time.perf_counter()
     if pool is None:
@@ -194,6 +203,69 @@ def run_reference(args):
                                        f"of {per} of the 4096 patches; bound&split single-threaded per process"},
             "e2e": {"value": value, "unit": "micropolygons/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
+    return 0
+
+
+def all_configs(args):
+    """One JSON line per workload of micropolis_gb300.scenes.WORKLOADS: the
+    batched path (autotuned knobs), the plain per-pass path, the oracle on all
+    host cores (one frame shared over the cores), and for the displaced
+    heightfields the backward / forward ratio."""
+    import torch
+    from micropolis_gb300 import adjoint, autotune, scenes
+    from micropolis_gb300.renderer import render_scene, renderer_for
+    stream = torch.cuda.Stream()
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    peak_gbs, peak_kind = measured_peaks()
+    cores = os.cpu_count() or 1
+    pool = cpu_pool(cores)
+    pool.map(_cpu_chunk, [("heightfield_1024x768", [(0, 1)])] * cores)
+    atom_peak = None
+    for name, make in scenes.WORKLOADS.items():
+        if args.workload and name not in args.workload:
+            continue
+        sc = make()
+        tuned = autotune.tune(sc, frames=3, warmup=1, use_cache=False)
+        line = {"workload": name, "patches": sc.n_patches, "width": sc.width, "height": sc.height,
+                "views": 1 + max(d.view for d in sc.draws), "tuned": tuned.best}
+        for path, over in (("batched", tuned.best), ("plain", {})):
+            r = renderer_for(sc, path, **over)
+            r.set_stream(stream.cuda_stream)
+            render_scene(r, sc)
+            if atom_peak is None:
+                kp = ((1920 + 31) // 32 * 32) * ((1080 + 31) // 32 * 32)
+                atom_peak = r.atomic_bench(kp, 1 << 27, 1)
+            ms = []
+            for _ in range(5 if path == "batched" else 3):
+                with torch.cuda.stream(stream):
+                    flush.fill_(1.0)
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                render_scene(r, sc)
+                b.record(stream)
+                torch.cuda.synchronize()
+                ms.append(a.elapsed_time(b))
+            st = r.stats()
+            m = statistics.median(ms)
+            cp_alg = sum(d.mesh.n_patches * d.mesh.cp.shape[1] * 12 for d in sc.draws)
+            views = line["views"]
+            frame_bytes = cp_alg + st["subpatches"] * 20 + views * sc.width * sc.height * (8 + 8 + 16)
+            line[path] = {"ms_per_frame": m, "micropolygons": st["micropolygons"],
+                          "value": st["micropolygons"] / (m / 1e3), "subpatches": st["subpatches"],
+                          "fragments": st["fragments"], "passes": st["passes"], "kernels": st["kernels"],
+                          "frac_hbm": frame_bytes / (m / 1e3) / 1e9 / peak_gbs,
+                          "frac_atomic": st["fragments"] / (m / 1e3) / atom_peak}
+            r.close()
+        line["batched_over_plain"] = line["batched"]["value"] / line["plain"]["value"]
+        cv, cmp, cwall, cbusy = cpu_baseline(name, cores, 0, pool)
+        line["cpu_baseline"] = {"value": cv, "unit": "micropolygons/s", "cores": cores, "kind": "port",
+                                "sample": f"one frame shared over {cores} processes ({cmp} micropolygons, "
+                                          f"busiest process {cbusy:.2f} s)"}
+        if sc.options.get("displacement"):
+            line["adjoint"] = adjoint.bench_bwd_fwd(stream, workload=name, steps=5)
+        line["peaks"] = {"hbm_gbs": peak_gbs, "hbm_kind": peak_kind, "atomic_per_s": atom_peak}
+        print(json.dumps(line), flush=True)
+    pool.close()
     return 0
 
 
@@ -245,6 +317,8 @@ def main():
 
     from micropolis_gb300 import build as mpbuild
     mpbuild.build()
+    if args.all_configs:
+        return all_configs(args) if rank == 0 else 0
     from micropolis_gb300 import scenes
     from micropolis_gb300.renderer import Projection, renderer_for
 

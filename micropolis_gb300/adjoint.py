@@ -74,17 +74,20 @@ def render(cp: torch.Tensor, amp: torch.Tensor, dr: DiffRenderer) -> torch.Tenso
     return RenderFunction.apply(cp, amp, dr)
 
 
-def bench_bwd_fwd(stream=None, steps: int = 10) -> dict:
-    """Forward (frame) and backward (adjoint) device times on the displaced
-    16x16 heightfield at 512x512 with an L2 image loss against a perturbed target."""
+def bench_bwd_fwd(stream=None, steps: int = 10, workload: str = "heightfield16_512x512") -> dict:
+    """Forward (frame) and backward (adjoint) device times on a displaced
+    heightfield workload (default the 16x16 one at 512x512) with an L2 image
+    loss against a target rendered from perturbed control points: N(0, 0.05)
+    for 16 x 16 patches, scaled with the patch spacing for finer grids."""
     import numpy as np
     from . import scenes
-    sc = scenes.heightfield16_512x512()
+    sc = scenes.WORKLOADS[workload]()
     dev = torch.device("cuda")
     dr = DiffRenderer(sc)
     cp0 = torch.tensor(sc.draws[0].mesh.cp, device=dev)
     rng = np.random.default_rng(sc.seed + 100)
-    cpt = cp0 + torch.tensor(rng.normal(0, 0.05, size=cp0.shape).astype(np.float32), device=dev)
+    sigma = 0.05 * 16.0 / max(16.0, float(np.sqrt(sc.n_patches)))
+    cpt = cp0 + torch.tensor(rng.normal(0, sigma, size=cp0.shape).astype(np.float32), device=dev)
     target = dr.render(cpt, 1.2).clone()
     cp = cp0.clone().requires_grad_(True)
     amp = torch.tensor(1.0, device=dev, requires_grad=True)
@@ -106,5 +109,4 @@ def bench_bwd_fwd(stream=None, steps: int = 10) -> dict:
             bwd.append(b2.elapsed_time(c))
         del loss
     f, bk = float(np.median(fwd)), float(np.median(bwd))
-    return {"workload": "heightfield16_512x512 (displacement on)", "fwd_ms": f, "bwd_ms": bk,
-            "bwd_over_fwd": bk / f}
+    return {"workload": f"{workload} (displacement on)", "fwd_ms": f, "bwd_ms": bk, "bwd_over_fwd": bk / f}

@@ -114,35 +114,36 @@ __device__ __forceinline__ void bns_warp_loop(const DrawDev* draws, const int* _
             }
             dec = bns_decide(draws[draw], fr, pid, r, depth);
         }
-        // emitted sub-patches
-        unsigned emask = __ballot_sync(0xffffffffu, dec == kDraw);
-        if (emask) {
-            int leader = __ffs(emask) - 1;
-            unsigned long long base = 0;
-            if (lane == leader) base = atomicAdd(cw(ctrl, kOutCount), (unsigned long long)__popc(emask));
-            base = __shfl_sync(0xffffffffu, base, leader);
-            if (dec == kDraw) {
-                unsigned long long o = base + __popc(emask & lanemask_lt());
-                if ((long long)o < out.capacity) {
-                    out.range[o] = r;
-                    out.meta[o] = make_int2(pid, draw);
-                    // consumers running in the same launch wait for this flag
-                    if (out_seq) st_release_u32(out_seq + o, epoch);
-                } else {
-                    set_status(ctrl, kErrOverflow);
-                }
-            }
-        }
-        // split children: reserve their tickets and account this step's work
-        // with one packed atomic (see kQTail above)
+        // One lane issues the step's three independent atomics back to back,
+        // so their round trips overlap: output slots for emitted sub-patches,
+        // the packed ticket / outstanding-work update for split children (see
+        // kQTail above), and the next tickets of the lanes finished here.
+        const unsigned emask = __ballot_sync(0xffffffffu, dec == kDraw);
         const bool split = dec == kSplitX || dec == kSplitY;
         const unsigned smask = __ballot_sync(0xffffffffu, split);
         const long long n_child = 2ll * __popc(smask);
         const long long net = n_child - (long long)__popc(rmask);
-        unsigned long long old = 0;
-        if (lane == 0)
+        unsigned long long obase = 0, old = 0, tbase = 0;
+        if (lane == 0) {
+            if (emask) obase = atomicAdd(cw(ctrl, kOutCount), (unsigned long long)__popc(emask));
             old = atomicAdd(cw(ctrl, kQTail), ((unsigned long long)n_child << 32) + (unsigned long long)net);
+            tbase = atomicAdd(cw(ctrl, kQHead), (unsigned long long)__popc(rmask));
+        }
+        obase = __shfl_sync(0xffffffffu, obase, 0);
         old = __shfl_sync(0xffffffffu, old, 0);
+        tbase = __shfl_sync(0xffffffffu, tbase, 0);
+        // emitted sub-patches
+        if (dec == kDraw) {
+            unsigned long long o = obase + __popc(emask & lanemask_lt());
+            if ((long long)o < out.capacity) {
+                out.range[o] = r;
+                out.meta[o] = make_int2(pid, draw);
+                // consumers running in the same launch wait for this flag
+                if (out_seq) st_release_u32(out_seq + o, epoch);
+            } else {
+                set_status(ctrl, kErrOverflow);
+            }
+        }
         bool fits = true;
         if (split) {
             const unsigned long long t0 = (old >> 32) + 2ull * __popc(smask & lanemask_lt());
@@ -174,7 +175,7 @@ __device__ __forceinline__ void bns_warp_loop(const DrawDev* draws, const int* _
             }
             if (remaining == 0) st_release_u64(cw(ctrl, kDone), 1ull);
         }
-        if (ready) ticket = kNoTicket;
+        if (ready) ticket = tbase + __popc(rmask & lanemask_lt());
     }
 }
 
