@@ -142,9 +142,12 @@ mp_status mp_finish(mp_ctx* ctx);
  * launches with CUDA events between them instead of one graph replay, and
  * mp_stats.stage_ms is filled (for profiling; the graph replay is faster). */
 mp_status mp_set_stage_timing(mp_ctx* ctx, int32_t on);
-/* Renderer::dump_trace (Renderer.h:43): per-stage device times of the last frame
- * as `name@queue:queued:submit:start:end:id:` lines (src/CL/Device.cpp:275-289)
- * into buf (NUL-terminated, truncated to cap). */
+/* Renderer::dump_trace (Renderer.h:43): the last frame's device commands as
+ * `name@queue:queued:submit:start:end:id:deps` lines (src/CL/Device.cpp:275-289),
+ * times in ns from the start of the frame, deps '|'-separated ids.  With stage
+ * timing on (mp_set_stage_timing) one line per stage (per pass on the plain
+ * path), else one line for the frame.  NUL-terminated; MP_ERR_OVERFLOW when
+ * the text did not fit in cap bytes (buf then holds the lines that fit). */
 mp_status mp_dump_trace(mp_ctx* ctx, char* buf, size_t cap);
 
 /* Headless framebuffer (replaces OGLSharedFramebuffer, src/Reyes/Framebuffer.cpp:75-144):
@@ -199,6 +202,17 @@ mp_status mp_inclusive_scan(mp_ctx* ctx, const int32_t* host_in, int32_t* host_o
  * that overlap on the GPU race and must be serialized by the caller.  Runs on
  * `stream` (a cudaStream_t, NULL = default stream) and returns when done. */
 mp_status mp_inclusive_scan_noalloc(const int32_t* in_dev, int32_t* out_dev, int64_t n, void* stream);
+
+/* The image the reference shows for one layer (shaders/tex_draw.frag: gamma
+ * 1/2.2 on RGB, 8-bit window): W*H*3 bytes, RGB, top row first.  Replaces the
+ * OpenGL presentation of OGLSharedFramebuffer::show (src/Reyes/Framebuffer.cpp)
+ * with a host buffer. */
+mp_status mp_read_image(mp_ctx* ctx, int32_t view, uint8_t* rgb);
+
+/* Statistics of the last frame in the format of Statistics::dump_stats
+ * (src/base/Statistics.cpp:196-217): "key = value;" lines.  Writes at most
+ * cap bytes including the terminating zero; MP_ERR_OVERFLOW when truncated. */
+mp_status mp_dump_stats(mp_ctx* ctx, char* buf, size_t cap);
 
 /* 64-bit atomicMin throughput probe (atomics per second): pattern 0 uniform
  * random slots, pattern 1 micropolygon-like locality. */

@@ -77,6 +77,8 @@ SIGNATURES = [
     ("mp_inclusive_scan", ctypes.c_int, [c_void_p, P(i32), P(i32), i64]),
     ("mp_inclusive_scan_noalloc", ctypes.c_int, [c_void_p, c_void_p, i64, c_void_p]),
     ("mp_atomic_bench", ctypes.c_int, [c_void_p, i64, i64, i32, P(ctypes.c_double)]),
+    ("mp_read_image", ctypes.c_int, [c_void_p, i32, P(ctypes.c_uint8)]),
+    ("mp_dump_stats", ctypes.c_int, [c_void_p, ctypes.c_char_p, ctypes.c_size_t]),
 ]
 
 _lib = None

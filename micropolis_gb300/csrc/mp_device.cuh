@@ -167,10 +167,37 @@ __device__ __forceinline__ void bbox_add(RangeBound& b, const F3& p) {
 // (0 + d01) + d12, the row sums h_iu accumulate across columns in the same
 // order, vlen/hlen take maximum() in index order 0, 1, 2, and the bbox
 // (minimum/maximum that skip NaN) does not depend on the visiting order.
-__device__ __forceinline__ RangeBound bound_range(const DrawDev& d, int pid, float4 r) {
+// Eye-space points of the samples (iu, iv), iu = 0..2, of one column iv of
+// the 3x3 grid.
+__device__ __forceinline__ void bound_column(const DrawDev& d, int pid, float4 r, int iv, F3 cur[3]) {
     float sv[3];
 #pragma unroll
     for (int i = 0; i < 3; ++i) sv[i] = fadd(r.x, fmul(fmul(fsub(r.z, r.x), (float)i), 0.5f));
+    const float su_iv = fadd(r.y, fmul(fmul(fsub(r.w, r.y), (float)iv), 0.5f));
+    if (d.type == 0) {
+        // eval_patch(P, t = u, s = v): rows P[i][0..3] in t, then the column in s
+        const float4* P = d.cp + (size_t)pid * 16;
+        SplineW wt = spline_weights(su_iv);
+        F3 row[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+            row[i] = spline3(wt, ld3(P + 4 * i + 0), ld3(P + 4 * i + 1), ld3(P + 4 * i + 2), ld3(P + 4 * i + 3));
+#pragma unroll
+        for (int iu = 0; iu < 3; ++iu)
+            cur[iu] = mv_point(d.mv, spline3(spline_weights(sv[iu]), row[0], row[1], row[2], row[3]));
+    } else {
+        const float4* P = d.cp + (size_t)pid * 20;
+#pragma unroll
+        for (int iu = 0; iu < 3; ++iu) cur[iu] = mv_point(d.mv, eval_gregory_cpu(P, su_iv, sv[iu]));
+    }
+}
+
+// column iv's summed distance: v = (0 + d(ps[0][iv], ps[1][iv])) + d(ps[1][iv], ps[2][iv])
+__device__ __forceinline__ float column_length(const F3 cur[3]) {
+    return fadd(fadd(0.0f, distance3(cur[0], cur[1])), distance3(cur[1], cur[2]));
+}
+
+__device__ __forceinline__ RangeBound bound_range(const DrawDev& d, int pid, float4 r) {
     RangeBound b;
     const float inf = __int_as_float(0x7f800000);
     b.bmin = F3{inf, inf, inf};
@@ -181,28 +208,10 @@ __device__ __forceinline__ RangeBound bound_range(const DrawDev& d, int pid, flo
 #pragma unroll 1
     for (int iv = 0; iv < 3; ++iv) {
         F3 cur[3];
-        const float su_iv = fadd(r.y, fmul(fmul(fsub(r.w, r.y), (float)iv), 0.5f));
-        if (d.type == 0) {
-            // eval_patch(P, t = u, s = v): rows P[i][0..3] in t, then the column in s
-            const float4* P = d.cp + (size_t)pid * 16;
-            SplineW wt = spline_weights(su_iv);
-            F3 row[4];
-#pragma unroll
-            for (int i = 0; i < 4; ++i)
-                row[i] = spline3(wt, ld3(P + 4 * i + 0), ld3(P + 4 * i + 1), ld3(P + 4 * i + 2), ld3(P + 4 * i + 3));
-#pragma unroll
-            for (int iu = 0; iu < 3; ++iu)
-                cur[iu] = mv_point(d.mv, spline3(spline_weights(sv[iu]), row[0], row[1], row[2], row[3]));
-        } else {
-            const float4* P = d.cp + (size_t)pid * 20;
-#pragma unroll
-            for (int iu = 0; iu < 3; ++iu) cur[iu] = mv_point(d.mv, eval_gregory_cpu(P, su_iv, sv[iu]));
-        }
+        bound_column(d, pid, r, iv, cur);
 #pragma unroll
         for (int iu = 0; iu < 3; ++iu) bbox_add(b, cur[iu]);
-        // column iv: v = (0 + d(ps[0][iv], ps[1][iv])) + d(ps[1][iv], ps[2][iv])
-        float v = fadd(fadd(0.0f, distance3(cur[0], cur[1])), distance3(cur[1], cur[2]));
-        b.vlen = maximum(v, b.vlen);
+        b.vlen = maximum(column_length(cur), b.vlen);
         if (iv > 0) {
 #pragma unroll
             for (int iu = 0; iu < 3; ++iu) hsum[iu] = fadd(hsum[iu], distance3(prev[iu], cur[iu]));
@@ -239,13 +248,15 @@ enum BnsDecision { kCull = 0, kDraw = 1, kSplitY = 2, kSplitX = 3, kDrop = 4 };
 // src/Reyes/BoundNSplitCLCPU.cpp:117-148: cull, draw when in front of the eye
 // and smaller than the limit, drop past the depth cap, otherwise split the
 // direction with the longer sampled length (vlen < hlen halves y).
-__device__ __forceinline__ int bns_decide(const DrawDev& d, const FrameDev& fr, int pid, float4 r, int depth) {
-    RangeBound b = bound_range(d, pid, r);
+__device__ __forceinline__ int bns_decide_bound(const DrawDev& d, const FrameDev& fr, const RangeBound& b, int depth) {
     float sx, sy;
     if (projection_cull(d, b, sx, sy)) return kCull;
     if (b.bmin.z < 0 && sx < fr.limit && sy < fr.limit) return kDraw;
     if (depth > fr.max_depth) return kDrop;
     return (b.vlen < b.hlen) ? kSplitY : kSplitX;
+}
+__device__ __forceinline__ int bns_decide(const DrawDev& d, const FrameDev& fr, int pid, float4 r, int depth) {
+    return bns_decide_bound(d, fr, bound_range(d, pid, r), depth);
 }
 
 // Children of a split (BoundNSplitCLCPU.cpp:231-245): low half, high half.

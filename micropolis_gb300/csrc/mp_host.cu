@@ -10,6 +10,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdarg>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -96,6 +97,15 @@ struct mp_ctx {
     cudaEvent_t sev[8] = {};
     mp_stats stats{};
     long long plain_bounds = 0, plain_passes = 0, plain_out = 0, plain_kernels = 0;
+    long long plain_max_stack = 0;
+    // stage events of the last frame (stage timing on): name, start, end in ns from the frame start
+    struct TraceEvent {
+        const char* name;
+        long long start, end;
+    };
+    std::vector<TraceEvent> trace;
+    unsigned char* image = nullptr;   // device buffer of mp_read_image
+    long long image_bytes = 0;
 };
 
 namespace {
@@ -318,6 +328,7 @@ mp_status plain_draw(mp_ctx* c, int draw_index) {
             st = grow_sub(c, c->plain_out + b, true);
             if (st) return st;
         }
+        c->plain_max_stack = std::max(c->plain_max_stack, h + b);
         if (c->stage_timing) CK(cudaEventRecord(c->sev[0], c->stream));
         launch_bns_pass(c->d_draws, c->fr, c->stack, h, (int)b, c->pad_range, c->pad_meta, c->dec, c->keys,
                         c->scan_state, c->sub, c->plain_out, c->ctrl, c->opt.spin_limit, c->stream);
@@ -326,9 +337,11 @@ mp_status plain_draw(mp_ctx* c, int draw_index) {
         if (c->stage_timing) CK(cudaEventRecord(c->sev[1], c->stream));
         st = read_ctrl(c);
         if (c->stage_timing) {
-            float ms = 0;
+            float ms = 0, t0 = 0;
             cudaEventElapsedTime(&ms, c->sev[0], c->sev[1]);
+            cudaEventElapsedTime(&t0, c->ev0, c->sev[0]);
             c->stats.stage_ms[1] += ms;
+            c->trace.push_back({"bound & split", (long long)(t0 * 1e6), (long long)((t0 + ms) * 1e6)});
         }
         if (st) return st;
         if (hc(c, kStatus)) return check_status(c, hc(c, kStatus));
@@ -361,9 +374,14 @@ mp_status plain_draw(mp_ctx* c, int draw_index) {
                 CK(cudaEventSynchronize(c->sev[7]));
                 float ms = 0;
                 const int slot[5] = {2, 4, 5, 3, 6};  // dice, shade, sample, slow raster, pass resolve
+                // command names of the reference's trace (tools/trace_summary.py maps these)
+                static const char* const names[5] = {"dice", "shade", "sample", "sample", "sample"};
                 for (int k = 0; k < 5; ++k) {
+                    float t0 = 0;
                     cudaEventElapsedTime(&ms, c->sev[2 + k], c->sev[3 + k]);
+                    cudaEventElapsedTime(&t0, c->ev0, c->sev[2 + k]);
                     c->stats.stage_ms[slot[k]] += ms;
+                    c->trace.push_back({names[k], (long long)(t0 * 1e6), (long long)((t0 + ms) * 1e6)});
                 }
             }
             c->plain_out += n;
@@ -471,11 +489,18 @@ mp_status batched_frame(mp_ctx* c) {
                                cudaMemcpyDeviceToHost, c->stream));
             CK(cudaStreamSynchronize(c->stream));
             CK(cudaGetLastError());
-            float ms = 0;
+            float ms = 0, t = 0;
             cudaEvent_t prev = c->ev0;
+            // command names of the reference's trace (tools/trace_summary.py maps these): the fused
+            // dice+shade+raster launch is reported as dice, the exact slow raster as sample and
+            // the colour resolve as shade
+            static const char* const names[5] = {"clear framebuffer", "bound & split", "dice", "sample", "shade"};
+            c->trace.clear();
             for (int k = 0; k < 5; ++k) {
                 cudaEventElapsedTime(&ms, prev, c->sev[k]);
                 c->stats.stage_ms[k] = ms;
+                c->trace.push_back({names[k], (long long)(t * 1e6), (long long)((t + ms) * 1e6)});
+                t += ms;
                 prev = c->sev[k];
             }
         } else {
@@ -689,6 +714,7 @@ void mp_destroy(mp_ctx* c) {
     dfree(c->stack.range); dfree(c->stack.meta);
     dfree(c->pad_range); dfree(c->pad_meta); dfree(c->dec); dfree(c->keys); dfree(c->scan_state);
     dfree(c->pos_grid); dfree(c->pxl_grid); dfree(c->depth_grid); dfree(c->color_grid); dfree(c->block_index);
+    dfree(c->image);
     for (auto& e : c->sev)
         if (e) cudaEventDestroy(e);
     if (c->ev0) cudaEventDestroy(c->ev0);
@@ -818,6 +844,8 @@ mp_status mp_prepare(mp_ctx* c) {
     c->draws.clear();
     c->plain_bounds = c->plain_passes = c->plain_out = 0;
     c->plain_kernels = 0;
+    c->plain_max_stack = 0;
+    c->trace.clear();
     for (double& v : c->stats.stage_ms) v = 0;
     if (c->opt.path == MP_PATH_PLAIN) {
         CK(cudaEventRecord(c->ev0, c->stream));
@@ -900,11 +928,97 @@ mp_status mp_set_stage_timing(mp_ctx* c, int32_t on) {
     return MP_OK;
 }
 
+// Appends printf-formatted text at *pos; false once the buffer is full.
+bool put(char* buf, size_t cap, size_t* pos, const char* fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    const int n = std::vsnprintf(buf + *pos, cap - *pos, fmt, ap);
+    va_end(ap);
+    if (n < 0 || (size_t)n >= cap - *pos) {
+        buf[*pos] = 0;
+        return false;
+    }
+    *pos += (size_t)n;
+    return true;
+}
+
 mp_status mp_dump_trace(mp_ctx* c, char* buf, size_t cap) {
     if (!c || !buf || cap == 0) return MP_ERR_INVALID_ARG;
-    // one line per frame in the reference's event format (src/CL/Device.cpp:275-289)
-    long long end_ns = (long long)(c->stats.gpu_ms * 1e6);
-    std::snprintf(buf, cap, "frame@%s:0:0:0:%lld:0:\n", c->opt.path == MP_PATH_PLAIN ? "plain" : "batched", end_ns);
+    buf[0] = 0;
+    size_t pos = 0;
+    const char* queue = c->opt.path == MP_PATH_PLAIN ? "plain" : "batched";
+    if (c->trace.empty()) {
+        const long long end_ns = (long long)(c->stats.gpu_ms * 1e6);
+        if (!put(buf, cap, &pos, "frame@%s:0:0:0:%lld:0:\n", queue, end_ns)) return MP_ERR_OVERFLOW;
+        return MP_OK;
+    }
+    for (size_t i = 0; i < c->trace.size(); ++i) {
+        const auto& e = c->trace[i];
+        // each command depends on the one before it on the stream
+        bool ok = i == 0 ? put(buf, cap, &pos, "%s@%s:%lld:%lld:%lld:%lld:%zu:\n", e.name, queue, e.start, e.start,
+                               e.start, e.end, i)
+                         : put(buf, cap, &pos, "%s@%s:%lld:%lld:%lld:%lld:%zu:%zu\n", e.name, queue, e.start, e.start,
+                               e.start, e.end, i, i - 1);
+        if (!ok) return MP_ERR_OVERFLOW;
+    }
+    return MP_OK;
+}
+
+mp_status mp_dump_stats(mp_ctx* c, char* buf, size_t cap) {
+    if (!c || !buf || cap == 0) return MP_ERR_INVALID_ARG;
+    buf[0] = 0;
+    // device memory by use (the reference's opencl_memory_by_use)
+    long long cp = 0, input = 0;
+    for (const auto& m : c->meshes) cp += (long long)m.second.n_points * (long long)sizeof(float4);
+    for (const auto& d : c->draws) input += d.n_patches;
+    const long long G2 = (long long)(c->fr.PS + 1) * (c->fr.PS + 1), Q = (long long)c->fr.PS * c->fr.PS;
+    const struct {
+        const char* use;
+        long long bytes;
+    } mem[] = {
+        {"control points", cp},
+        {"work queue", c->q.capacity * (long long)(sizeof(float4) + sizeof(uint2) + sizeof(unsigned))},
+        {"sub-patch list", c->sub.capacity * (long long)(sizeof(float4) + sizeof(int2) + sizeof(unsigned))},
+        {"diffuse factors", c->mshade_cap * (long long)sizeof(float)},
+        {"framebuffer", c->fb.key_pixels * c->fb.views * 8 + c->fb.pixels * c->fb.views * 20},
+        {"exact slow raster quads", c->big_cap * (long long)sizeof(BigQuad)},
+        {"bound and split stack", c->stack.capacity * (long long)(sizeof(float4) + sizeof(uint2))},
+        {"pass grids", c->pass_cap * (G2 * (16 + 8 + 4) + Q * 16 + (Q / 64) * 16 + 16 + 8 + 1 + 8)},
+        {"image", c->image_bytes},
+    };
+    long long total = 0;
+    for (const auto& m : mem) total += m.bytes;
+    size_t pos = 0;
+    bool ok = put(buf, cap, &pos, "opencl_mem = %lld;\n", total);
+    for (const auto& m : mem)
+        if (m.bytes > 0) ok = ok && put(buf, cap, &pos, "opencl_mem@%s = %lld;\n", m.use, m.bytes);
+    const long long max_patches = c->opt.path == MP_PATH_PLAIN
+                                      ? c->plain_max_stack
+                                      : (long long)(hc(c, kQTail) >> 32) - (long long)hc(c, kRoots);
+    ok = ok && put(buf, cap, &pos, "opengl_mem = 0;\n");
+    ok = ok && put(buf, cap, &pos, "max_patches = %lld;\n", max_patches);
+    ok = ok && put(buf, cap, &pos, "patches_per_frame = %lld;\n", (long long)c->stats.subpatches);
+    ok = ok && put(buf, cap, &pos, "processed_patches_per_frame = %lld;\n", (long long)c->stats.bounds);
+    ok = ok && put(buf, cap, &pos, "pass_count = %lld;\n", (long long)c->stats.passes);
+    ok = ok && put(buf, cap, &pos, "total_input_patches = %lld;\n", input);
+    ok = ok && put(buf, cap, &pos, "bound_n_split_balance = ;");
+    return ok ? MP_OK : MP_ERR_OVERFLOW;
+}
+
+mp_status mp_read_image(mp_ctx* c, int32_t view, uint8_t* rgb) {
+    if (!c || !rgb || view < 0 || view >= c->fb.views) return MP_ERR_INVALID_ARG;
+    const long long n = (long long)c->fr.W * c->fr.H * 3;
+    if (c->image_bytes < n) {
+        dfree(c->image);
+        c->image = nullptr;
+        c->image_bytes = 0;
+        CK(dalloc(&c->image, n));
+        c->image_bytes = n;
+    }
+    launch_image(c->fb.color + view * c->fb.pixels, c->fr, c->image, c->stream);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(rgb, c->image, (size_t)n, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
     return MP_OK;
 }
 

@@ -118,6 +118,7 @@ void launch_adjoint(const DrawDev* draws, const FrameDev& fr, const SubPatches& 
                     const float4* grad_color, float* grad_amp, int view, cudaStream_t s);
 
 // ---- microbenchmark (mp_raster.cu)
+void launch_image(const float4* color, const FrameDev& fr, unsigned char* rgb, cudaStream_t s);
 void launch_atomic_bench(unsigned long long* buf, long long n_slots, long long n_ops, int pattern, cudaStream_t s);
 
 }  // namespace mp

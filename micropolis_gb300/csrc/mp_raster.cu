@@ -746,6 +746,24 @@ __global__ void pass_resolve_kernel(FrameDev fr, Framebuffer fb, unsigned long l
     }
 }
 
+// Display image of one framebuffer layer, as the reference's tex_draw shader
+// shows it (shaders/tex_draw.frag): untile, gamma pow(c, 0.454545) on RGB,
+// then the unorm8 conversion of an 8-bit window (round(clamp(c, 0, 1) * 255)).
+// Rows are written top first; the shader's gl_FragCoord.y counts from the
+// bottom, so output row r is framebuffer row H - 1 - r.
+__global__ void image_kernel(const float4* __restrict__ color, FrameDev fr, unsigned char* __restrict__ rgb) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (long long)fr.W * fr.H) return;
+    const int x = (int)(i % fr.W), r = (int)(i / fr.W);
+    const float4 c = color[fb_index(fr, x, fr.H - 1 - r)];
+    const float v[3] = {c.x, c.y, c.z};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float g = fminf(fmaxf(powf(v[k], 0.454545f), 0.0f), 1.0f);
+        rgb[3 * i + k] = (unsigned char)__float2int_rn(fmul(g, 255.0f));
+    }
+}
+
 // 64-bit atomicMin throughput probe: pattern 0 = uniform random slots,
 // pattern 1 = each warp updates one 8x8-pixel tile (micropolygon-like locality).
 __global__ void atomic_bench_kernel(unsigned long long* buf, long long n_slots, long long n_ops, int pattern) {
@@ -907,6 +925,11 @@ void launch_pass_resolve(const FrameDev& fr, const Framebuffer& fb, long long ba
 void launch_dice_debug(const DrawDev* draws, const FrameDev& fr, const SubPatches& sub, int count, float4* pos,
                        int2* pxl, float* depth, cudaStream_t s) {
     launch_dice_grid(draws, fr, sub, 0, count, pos, pxl, depth, s);
+}
+
+void launch_image(const float4* color, const FrameDev& fr, unsigned char* rgb, cudaStream_t s) {
+    const long long n = (long long)fr.W * fr.H;
+    image_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(color, fr, rgb);
 }
 
 void launch_atomic_bench(unsigned long long* buf, long long n_slots, long long n_ops, int pattern, cudaStream_t s) {

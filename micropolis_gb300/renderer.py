@@ -131,10 +131,31 @@ class Renderer:
         p = projection.c()
         self._ck(lib().mp_draw_patches_view(self._ctx, handle, _f32p(mv), ctypes.byref(p), _f32p(col), view))
 
+    def _text(self, fn) -> str:
+        size = 4096
+        while True:
+            buf = ctypes.create_string_buffer(size)
+            st = fn(self._ctx, buf, len(buf))
+            if st != _lib.MP_ERR_OVERFLOW:
+                self._ck(st)
+                return buf.value.decode()
+            size *= 4
+
     def dump_trace(self) -> str:
-        buf = ctypes.create_string_buffer(4096)
-        self._ck(lib().mp_dump_trace(self._ctx, buf, len(buf)))
-        return buf.value.decode()
+        """The last frame's commands in the reference's trace line format."""
+        return self._text(lib().mp_dump_trace)
+
+    def dump_stats(self) -> str:
+        """The last frame's statistics in the format of Statistics::dump_stats."""
+        return self._text(lib().mp_dump_stats)
+
+    def write_trace(self, path: str) -> None:
+        with open(path, "w") as f:
+            f.write(self.dump_trace())
+
+    def write_stats(self, path: str) -> None:
+        with open(path, "w") as f:
+            f.write(self.dump_stats())
 
     # -- headless framebuffer and inspection -------------------------------------
     def framebuffer_ptrs(self):
@@ -148,6 +169,21 @@ class Renderer:
         depth = np.zeros(n, np.int32)
         self._ck(lib().mp_read_framebuffer(self._ctx, view, _f32p(color), _i32p(depth), int(linear)))
         return color, depth
+
+    def read_image(self, view: int = 0) -> np.ndarray:
+        """The displayed image (gamma 1/2.2, 8-bit), (height, width, 3) RGB, top row first."""
+        rgb = np.zeros((self.height, self.width, 3), np.uint8)
+        self._ck(lib().mp_read_image(self._ctx, view, rgb.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8))))
+        return rgb
+
+    def save_ppm(self, path: str, view: int = 0) -> None:
+        """Binary PPM (P6) of the displayed image."""
+        write_ppm(path, self.read_image(view))
+
+    def save_pfm(self, path: str, view: int = 0) -> None:
+        """Linear colour as a PFM (little-endian float RGB, bottom row first)."""
+        color, _ = self.read_framebuffer(view, linear=True)
+        write_pfm(path, color.reshape(self.height, self.width, 4)[:, :, :3])
 
     def copy_framebuffer_device(self, view: int, color_ptr: int, depth_ptr: int = 0) -> None:
         self._ck(lib().mp_copy_framebuffer_device(self._ctx, view, ctypes.c_void_p(color_ptr or None),
@@ -212,6 +248,33 @@ class Renderer:
         r = ctypes.c_double()
         self._ck(lib().mp_atomic_bench(self._ctx, n_slots, n_ops, pattern, ctypes.byref(r)))
         return r.value
+
+
+def write_ppm(path: str, rgb: np.ndarray) -> None:
+    """(height, width, 3) uint8 RGB, top row first, as binary PPM."""
+    h, w, _ = rgb.shape
+    with open(path, "wb") as f:
+        f.write(b"P6\n%d %d\n255\n" % (w, h))
+        f.write(np.ascontiguousarray(rgb, np.uint8).tobytes())
+
+
+def read_ppm(path: str) -> np.ndarray:
+    with open(path, "rb") as f:
+        data = f.read()
+    parts = data.split(maxsplit=4)
+    if parts[0] != b"P6" or int(parts[3]) != 255:
+        raise ValueError("not an 8-bit binary PPM")
+    w, h = int(parts[1]), int(parts[2])
+    return np.frombuffer(parts[4][:w * h * 3], np.uint8).reshape(h, w, 3)
+
+
+def write_pfm(path: str, rgb_rows_up: np.ndarray) -> None:
+    """(height, width, 3) float RGB whose row 0 is the bottom row (the
+    framebuffer's y axis), as PFM, which stores rows bottom first."""
+    h, w, _ = rgb_rows_up.shape
+    with open(path, "wb") as f:
+        f.write(b"PF\n%d %d\n-1.0\n" % (w, h))
+        f.write(np.ascontiguousarray(rgb_rows_up, "<f4").tobytes())
 
 
 def render_scene(renderer: Renderer, scene, handles=None) -> None:

@@ -263,3 +263,53 @@ def ref_bound_n_split(scene, draw_index=0, params=None):
     rng = np.zeros((max(n, 1), 4), np.float32)
     L.refpin_bound_n_split(*args, _ptr(pid, i32p), _ptr(rng, f32p), n)
     return pid[:n], rng[:n]
+
+
+def display_image(color_tiled, width, height, tile=8):
+    """The image the reference's tex_draw shader shows (shaders/tex_draw.frag):
+    pixel (x, y) of the framebuffer is texel (gx + ceil(W/tile) * gy) * tile^2
+    + lx + tile * ly; RGB gets pow(c, 0.454545); the 8-bit window stores
+    round(clamp(c, 0, 1) * 255).  gl_FragCoord.y counts from the bottom, so
+    the returned (height, width, 3) uint8 array has the top row first."""
+    c = np.asarray(color_tiled, np.float32).reshape(-1, 4)
+    gx = (width + tile - 1) // tile
+    y, x = np.mgrid[0:height, 0:width]
+    idx = ((x // tile) + gx * (y // tile)) * tile * tile + (x % tile) + tile * (y % tile)
+    rgb = c[idx.reshape(-1), :3].reshape(height, width, 3)
+    g = np.clip(np.power(rgb, np.float32(0.454545)), 0.0, 1.0).astype(np.float32)
+    out = np.rint(g * np.float32(255.0)).astype(np.uint8)
+    return out[::-1].copy()
+
+
+_TRACE_LINE = None
+
+
+def parse_trace(text):
+    """Lines of the reference's trace format (src/CL/Device.cpp:275-289), read
+    with the pattern of the reference's tools/parse_trace.py: a list of
+    (name, queue, queued, submit, start, end, id, deps)."""
+    import re
+    global _TRACE_LINE
+    if _TRACE_LINE is None:
+        _TRACE_LINE = re.compile(r'([^@:]*)(@[^@:]*):(\d+):(\d+):(\d+):(\d+):(\d+):([0-9|]*)')
+    out = []
+    for line in text.splitlines():
+        m = _TRACE_LINE.match(line)
+        if not m:
+            raise ValueError(f"trace line format mismatch: {line!r}")
+        out.append((m.group(1), m.group(2)[1:], int(m.group(3)), int(m.group(4)), int(m.group(5)), int(m.group(6)),
+                    int(m.group(7)), [int(s) for s in m.group(8).split('|') if s]))
+    return out
+
+
+def parse_stats(text):
+    """`key = value;` lines of Statistics::dump_stats (src/base/Statistics.cpp:196-217)."""
+    out = {}
+    for part in text.split(";"):
+        part = part.strip()
+        if not part:
+            continue
+        k, _, v = part.partition("=")
+        v = v.strip()
+        out[k.strip()] = [int(t) for t in v.split()] if k.strip() == "bound_n_split_balance" else int(v)
+    return out
