@@ -44,6 +44,20 @@ typedef enum {
 
 /* Options, named as in the reference's reyes.options (values there are the
  * defaults filled by mp_options_default). */
+/* Which bound criterion bound-and-split applies. */
+typedef enum {
+    /* the reference's CPU bound-and-split (src/Reyes/BoundNSplitCLCPU.cpp:117-148):
+     * eye-space 3x3 bbox projected by Projection::bound, strict < limit, split
+     * the direction with the longer eye-space arc length; the default, and the
+     * one the sub-patch set is bit-exact to */
+    MP_BOUND_CPU = 0,
+    /* the reference's GPU criterion (kernels/bound_n_split.h:43-100, used by
+     * its BOUNDED / LOCAL / BREADTH methods): screen-projected sample arc
+     * lengths with <=, the eye-plane split rule, far cull at 1000, cull at
+     * depth >= max_split_depth - 1; kernel arithmetic (R1-R6) */
+    MP_BOUND_GPU = 1
+} mp_bound_criterion;
+
 typedef struct {
     int32_t window_size[2];         /* framebuffer size; multiples of 8, at most 4096 */
     int32_t reyes_patch_size;       /* dice grid: 8 or 16 quads per side */
@@ -75,6 +89,8 @@ typedef struct {
      * (8, 16 or 22 at reyes_patch_size 8; 2, 4 or 6 at 16) */
     int32_t raster_tile;
     int32_t dice_group;
+    /* bound-and-split criterion (mp_bound_criterion) */
+    int32_t bound_criterion;
 } mp_options;
 
 /* The reference's Projection(fovy, near, viewport) (src/base/Projection.h:144). */

@@ -29,7 +29,8 @@ class MpOptions(ctypes.Structure):
                 ("clear_color", ctypes.c_float * 4), ("batch_views", ctypes.c_int32), ("path", ctypes.c_int32),
                 ("queue_capacity", ctypes.c_int64), ("subpatch_capacity", ctypes.c_int64),
                 ("spin_limit", ctypes.c_int64), ("overlap", ctypes.c_int32), ("bns_blocks", ctypes.c_int32),
-                ("raster_tile", ctypes.c_int32), ("dice_group", ctypes.c_int32)]
+                ("raster_tile", ctypes.c_int32), ("dice_group", ctypes.c_int32),
+                ("bound_criterion", ctypes.c_int32)]
 
 
 class MpProjection(ctypes.Structure):

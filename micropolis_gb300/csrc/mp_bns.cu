@@ -42,6 +42,7 @@ __global__ void bns_reset_kernel(unsigned long long* ctrl, long long roots) {
 constexpr int kBnsBlock = 128;
 constexpr int kBnsSmemDraws = 64;
 
+template <int CRIT>
 __global__ void __launch_bounds__(kBnsBlock) bns_persistent_kernel(const DrawDev* __restrict__ gdraws,
                                                                    const int* __restrict__ root_prefix,
                                                                    int n_draws, FrameDev fr, Queue q,
@@ -56,7 +57,7 @@ __global__ void __launch_bounds__(kBnsBlock) bns_persistent_kernel(const DrawDev
             reinterpret_cast<int*>(s_draws)[i] = __ldg(reinterpret_cast<const int*>(gdraws) + i);
         __syncthreads();
     }
-    bns_warp_loop(staged ? s_draws : gdraws, root_prefix, n_draws, fr, q, out, nullptr, ctrl, spin_limit);
+    bns_warp_loop<CRIT>(staged ? s_draws : gdraws, root_prefix, n_draws, fr, q, out, nullptr, ctrl, spin_limit);
 }
 
 // ---------------------------------------------------------------------------
@@ -79,6 +80,7 @@ constexpr unsigned long long kValMask = (1ull << 62) - 1;
 
 // bound kernel of one pass: decision, copy of the range to the pads, packed
 // scan key (draw + split << 31); also clears the scan state of this pass.
+template <int CRIT>
 __global__ void bns_pass_bound_kernel(const DrawDev* __restrict__ draws, FrameDev fr, Queue stack,
                                       long long offset, int batch, float4* pad_range, uint2* pad_meta,
                                       unsigned char* dec_out, unsigned long long* keys,
@@ -91,7 +93,7 @@ __global__ void bns_pass_bound_kernel(const DrawDev* __restrict__ draws, FrameDe
     float4 r = stack.range[offset + i];
     uint2 m = stack.meta[offset + i];
     int draw = (int)(m.y & 0xffffffu), depth = (int)(m.y >> 24);
-    int dec = bns_decide(draws[draw], fr, (int)m.x, r, depth);
+    int dec = bns_decide<CRIT>(draws[draw], fr, (int)m.x, r, depth);
     pad_range[i] = r;
     pad_meta[i] = m;
     dec_out[i] = (unsigned char)dec;
@@ -251,11 +253,14 @@ void launch_bns_reset(unsigned long long* ctrl, long long roots, cudaStream_t s)
     bns_reset_kernel<<<1, 1, 0, s>>>(ctrl, roots);
 }
 
-int bns_persistent_grid() {
+int bns_persistent_grid(int criterion) {
     int dev = 0, sms = 0, per_sm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, bns_persistent_kernel, kBnsBlock, 0);
+    if (criterion == 1)
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, bns_persistent_kernel<1>, kBnsBlock, 0);
+    else
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, bns_persistent_kernel<0>, kBnsBlock, 0);
     if (per_sm < 1) per_sm = 1;
     return sms * per_sm;
 }
@@ -263,7 +268,10 @@ int bns_persistent_grid() {
 void launch_bns_persistent(const DrawDev* draws, const int* root_prefix, int n_draws, const FrameDev& fr,
                            const Queue& q, const SubPatches& out, unsigned long long* ctrl, int grid,
                            long long spin_limit, cudaStream_t s) {
-    bns_persistent_kernel<<<grid, kBnsBlock, 0, s>>>(draws, root_prefix, n_draws, fr, q, out, ctrl, spin_limit);
+    if (fr.criterion == 1)
+        bns_persistent_kernel<1><<<grid, kBnsBlock, 0, s>>>(draws, root_prefix, n_draws, fr, q, out, ctrl, spin_limit);
+    else
+        bns_persistent_kernel<0><<<grid, kBnsBlock, 0, s>>>(draws, root_prefix, n_draws, fr, q, out, ctrl, spin_limit);
 }
 
 void launch_bns_init_stack(const Queue& stack, int draw, int n_patches, cudaStream_t s) {
@@ -280,8 +288,12 @@ void launch_bns_pass(const DrawDev* draws, const FrameDev& fr, const Queue& stac
     if (batch <= 0) return;
     long long n_tiles = scan_state_words(batch);
     int blocks = (batch + 127) / 128;
-    bns_pass_bound_kernel<<<blocks, 128, 0, s>>>(draws, fr, stack, offset, batch, pad_range, pad_meta, dec, keys,
-                                                 scan_state, n_tiles, ctrl);
+    if (fr.criterion == 1)
+        bns_pass_bound_kernel<1><<<blocks, 128, 0, s>>>(draws, fr, stack, offset, batch, pad_range, pad_meta, dec, keys,
+                                                        scan_state, n_tiles, ctrl);
+    else
+        bns_pass_bound_kernel<0><<<blocks, 128, 0, s>>>(draws, fr, stack, offset, batch, pad_range, pad_meta, dec, keys,
+                                                        scan_state, n_tiles, ctrl);
     int tiles = (int)((batch + kScanTileItems - 1) / kScanTileItems);
     scan_kernel<<<tiles, kScanBlock, 0, s>>>(keys, keys, batch, scan_state, ctrl, spin_limit, 0);
     bns_pass_move_kernel<<<(batch + 255) / 256, 256, 0, s>>>(pad_range, pad_meta, dec, keys, batch, stack, offset,

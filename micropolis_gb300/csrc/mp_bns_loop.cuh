@@ -45,7 +45,8 @@ constexpr unsigned long long kNoTicket = ~0ull;
 // Runs one warp's share of a frame's bound-and-split until the done flag is
 // raised.  Emitted sub-patches go to `out`; when out_seq is given, each
 // emitted slot is also marked with the frame's epoch (release) for consumers
-// that run concurrently.
+// that run concurrently.  CRIT selects the bound criterion (bns_decide).
+template <int CRIT>
 __device__ __forceinline__ void bns_warp_loop(const DrawDev* draws, const int* __restrict__ root_prefix, int n_draws,
                                               const FrameDev& fr, const Queue& q, const SubPatches& out,
                                               unsigned* out_seq, unsigned long long* ctrl, long long spin_limit) {
@@ -112,7 +113,7 @@ __device__ __forceinline__ void bns_warp_loop(const DrawDev* draws, const int* _
                 draw = (int)(m.y & 0xffffffu);
                 depth = (int)(m.y >> 24);
             }
-            dec = bns_decide(draws[draw], fr, pid, r, depth);
+            dec = bns_decide<CRIT>(draws[draw], fr, pid, r, depth);
         }
         // One lane issues the step's three independent atomics back to back,
         // so their round trips overlap: output slots for emitted sub-patches,

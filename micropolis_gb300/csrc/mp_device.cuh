@@ -42,6 +42,10 @@ struct DrawDev {
     float fx, fy, vpx, vpy;
     float near_plane, cull_ribbon;
     int vx, vy;
+    // GPU criterion: eps = near * 0.1 of kernels/bound_n_split.h:57, the
+    // product taken in double as the OpenCL source's double literal makes it
+    float near_eps;
+    int pad1[3];
 };
 
 // Frame-wide constants.
@@ -59,7 +63,7 @@ struct FrameDev {
     int n_draws;
     int kshift;            // depth|id key buffer tile: 1 << kshift pixels (8, 16 or 32)
     int kgx;               // key tiles per row
-    int pad1;
+    int criterion;         // mp_bound_criterion
 };
 
 // Depth|id key stored per pixel: (idepth << 32) | mp_id.  The clear key keeps
@@ -255,9 +259,7 @@ __device__ __forceinline__ int bns_decide_bound(const DrawDev& d, const FrameDev
     if (depth > fr.max_depth) return kDrop;
     return (b.vlen < b.hlen) ? kSplitY : kSplitX;
 }
-__device__ __forceinline__ int bns_decide(const DrawDev& d, const FrameDev& fr, int pid, float4 r, int depth) {
-    return bns_decide_bound(d, fr, bound_range(d, pid, r), depth);
-}
+
 
 // Children of a split (BoundNSplitCLCPU.cpp:231-245): low half, high half.
 __device__ __forceinline__ void split_children(float4 r, int dec, float4& c0, float4& c1) {
@@ -563,6 +565,80 @@ __device__ __forceinline__ void fb_pixel(const FrameDev& fr, long long i, int& x
 __device__ __forceinline__ long long key_index(const FrameDev& fr, int x, int y) {
     const int k = fr.kshift, m = (1 << k) - 1;
     return ((long long)((x >> k) + fr.kgx * (y >> k)) << (2 * k)) + (x & m) + ((y & m) << k);
+}
+
+// The reference's GPU bound criterion (kernels/bound_n_split.h:8-100), in the
+// kernel arithmetic (R1-R6).  The nine screen positions pp[v][u] are consumed
+// as they are produced: the sum along u of row v and the sum along v of
+// column u accumulate in the reference's order, so only the previous column
+// is kept.
+__device__ __forceinline__ int bns_decide_gpu(const DrawDev& d, const FrameDev& fr, int pid, float4 r, int depth) {
+    if (depth >= fr.max_depth - 1) return kCull;
+    const float inf = __int_as_float(0x7f800000);
+    float mnx = inf, mny = inf, mnz = inf, mxx = -inf, mxy = -inf, mxz = -inf;
+    float2 prev[3];                                  // pp[v][u - 1]
+    float hsum[3] = {0.0f, 0.0f, 0.0f};              // along u, per row v
+    float vlen = 0.0f;
+    const float4* P = d.cp + (size_t)pid * (d.type == 0 ? 16 : 20);
+#pragma unroll 1
+    for (int u = 0; u < 3; ++u) {
+        float vsum = 0.0f;                           // along v, column u
+        float2 above = make_float2(0.0f, 0.0f);      // pp[v - 1][u]
+#pragma unroll
+        for (int v = 0; v < 3; ++v) {
+            // uv = mix(rmin, rmax, (u, v) * (1 / (RES - 1)))
+            const float tx = ffma(fsub(r.z, r.x), fmul((float)u, 0.5f), r.x);
+            const float ty = ffma(fsub(r.w, r.y), fmul((float)v, 0.5f), r.y);
+            const float4 o = d.type == 0 ? eval_bezier_dice(P, tx, ty) : eval_gregory_dice(P, tx, ty);
+            const float4 p = mul_m44v4(d.mv, o);
+            mnx = fminf(mnx, p.x); mny = fminf(mny, p.y); mnz = fminf(mnz, p.z);
+            mxx = fmaxf(mxx, p.x); mxy = fmaxf(mxy, p.y); mxz = fmaxf(mxz, p.z);
+            const float4 q = mul_m44v4(d.proj, p);
+            const float rw = frcp(q.w);
+            const float x = fmul(q.x, rw), y = fmul(q.y, rw);
+            // mul_cm2v2(screen_matrix = diag(vp), (x, y)): m0 * x + m1 * y per component
+            const float2 s = make_float2(ffma(0.0f, y, fmul(d.vpx, x)), ffma(d.vpy, y, fmul(0.0f, x)));
+            // distance(a, b) = sqrt(dx*dx + dy*dy), R1: fma(dy, dy, dx*dx)
+            if (v > 0) {
+                const float dx = fsub(above.x, s.x), dy = fsub(above.y, s.y);
+                vsum = fadd(vsum, __fsqrt_rn(ffma(dy, dy, fmul(dx, dx))));
+            }
+            if (u > 0) {
+                const float dx = fsub(prev[v].x, s.x), dy = fsub(prev[v].y, s.y);
+                hsum[v] = fadd(hsum[v], __fsqrt_rn(ffma(dy, dy, fmul(dx, dx))));
+            }
+            above = s;
+            prev[v] = s;
+        }
+        vlen = fmaxf(vsum, vlen);
+    }
+    // outside_frustum (kernels/bound_n_split.h:8-30)
+    float n = -mxz;
+    const float f = -mnz;
+    if (f < d.near_plane || n > 1000.0f) return kCull;
+    n = fmaxf(d.near_plane, n);
+    const float sminx = ffma(kdiv(mnx, mnx < 0 ? n : f), d.fx, d.vpx);
+    const float sminy = ffma(kdiv(mny, mny < 0 ? n : f), d.fy, d.vpy);
+    const float smaxx = ffma(kdiv(mxx, mxx > 0 ? n : f), d.fx, d.vpx);
+    const float smaxy = ffma(kdiv(mxy, mxy > 0 ? n : f), d.fy, d.vpy);
+    if (sminx > fadd((float)(d.vx - 1), d.cull_ribbon) || smaxx < -d.cull_ribbon ||
+        sminy > fadd((float)(d.vy - 1), d.cull_ribbon) || smaxy < -d.cull_ribbon)
+        return kCull;
+    // straddles the eye plane: split the shorter parametric side (VSPLIT halves x)
+    if (mnz < d.near_eps && mxz > d.near_plane) return fsub(r.z, r.x) < fsub(r.w, r.y) ? kSplitX : kSplitY;
+    float hlen = 0.0f;
+#pragma unroll
+    for (int v = 0; v < 3; ++v) hlen = fmaxf(hsum[v], hlen);
+    if (hlen <= fr.limit && vlen <= fr.limit) return kDraw;
+    return hlen > vlen ? kSplitX : kSplitY;
+}
+
+// The decision of one range.  CRIT: 0 the CPU criterion, 1 the GPU
+// criterion, -1 chosen at run time from fr.criterion (one kernel for both).
+template <int CRIT>
+__device__ __forceinline__ int bns_decide(const DrawDev& d, const FrameDev& fr, int pid, float4 r, int depth) {
+    if (CRIT == 1 || (CRIT < 0 && fr.criterion == 1)) return bns_decide_gpu(d, fr, pid, r, depth);
+    return bns_decide_bound(d, fr, bound_range(d, pid, r), depth);
 }
 
 }  // namespace mp

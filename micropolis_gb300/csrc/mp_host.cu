@@ -393,6 +393,9 @@ mp_status plain_draw(mp_ctx* c, int draw_index) {
 // ---------------------------------------------------------------------------
 // batched path: the whole frame as one graph
 
+// The overlapped frame kernel carries the CPU bound criterion only.
+bool overlapped(const mp_ctx* c) { return c->opt.overlap && c->fr.criterion == MP_BOUND_CPU; }
+
 int bns_blocks(const mp_ctx* c) {
     if (c->opt.bns_blocks > 0) return std::min(c->opt.bns_blocks, c->frame_grid);
     return std::max(1, c->frame_grid / 3);
@@ -400,7 +403,7 @@ int bns_blocks(const mp_ctx* c) {
 
 // bound-and-split and rasterization: one overlapped launch or two launches
 void launch_middle(mp_ctx* c, int n) {
-    if (c->opt.overlap) {
+    if (overlapped(c)) {
         launch_frame_kernel(c->d_draws, c->d_root_prefix, n, c->fr, c->q, c->sub, c->fb, c->mshade, c->big, c->big_cap,
                             c->ctrl, c->opt.spin_limit, c->frame_grid, bns_blocks(c), c->opt.dice_group, c->stream);
     } else {
@@ -468,7 +471,7 @@ mp_status batched_frame(mp_ctx* c) {
             launch_bns_reset(c->ctrl, roots, c->stream);
             launch_clear(c->fb, c->fr, 0, c->stream);
             CK(cudaEventRecord(c->sev[0], c->stream));
-            if (c->opt.overlap) {
+            if (overlapped(c)) {
                 // one launch: reported under dice+raster, bound&split shows 0
                 CK(cudaEventRecord(c->sev[1], c->stream));
                 launch_middle(c, n);
@@ -559,6 +562,7 @@ mp_status fill_draw(mp_ctx* c, const Mesh& m, const float* mv, const mp_projecti
     d.fx = fx * d.vpx;
     d.fy = fy * d.vpy;
     d.near_plane = proj->near_plane;
+    d.near_eps = (float)((double)proj->near_plane * 0.1);
     d.cull_ribbon = c->opt.cull_ribbon;
     d.vx = W;
     d.vy = H;
@@ -623,6 +627,7 @@ mp_status mp_create(const mp_options* opts, mp_ctx** out) {
     if (o.reyes_patches_per_pass < 1 || o.batch_views < 1 || o.batch_views > 65536) return MP_ERR_INVALID_ARG;
     if (o.path != MP_PATH_PLAIN && o.path != MP_PATH_BATCHED) return MP_ERR_INVALID_ARG;
     if (o.spin_limit <= 0) o.spin_limit = 1 << 20;
+    if (o.bound_criterion != MP_BOUND_CPU && o.bound_criterion != MP_BOUND_GPU) return MP_ERR_INVALID_ARG;
     if (o.raster_tile == 0) o.raster_tile = 8;
     if (o.raster_tile != 8 && o.raster_tile != 16 && o.raster_tile != 32) return MP_ERR_INVALID_ARG;
     if (o.dice_group == 0) o.dice_group = o.reyes_patch_size == 16 ? 6 : 22;
@@ -671,6 +676,7 @@ mp_status mp_create(const mp_options* opts, mp_ctx** out) {
     c->fb.key_pixels = (long long)((W + 31) / 32 * 32) * ((H + 31) / 32 * 32);
     fr.kshift = o.raster_tile == 32 ? 5 : o.raster_tile == 16 ? 4 : 3;
     fr.kgx = (W + (1 << fr.kshift) - 1) >> fr.kshift;
+    fr.criterion = o.bound_criterion;
     ck(dalloc(&c->fb.keys, c->fb.key_pixels * c->fb.views), "fb keys");
     ck(dalloc(&c->fb.color, c->fb.pixels * c->fb.views), "fb color");
     ck(dalloc(&c->fb.depth, c->fb.pixels * c->fb.views), "fb depth");
@@ -680,7 +686,7 @@ mp_status mp_create(const mp_options* opts, mp_ctx** out) {
     if (st == MP_OK) st = ensure_draws(c, 4);
     if (st == MP_OK) st = grow_big(c, 1 << 16);
     if (st == MP_OK) {
-        c->bns_grid = bns_persistent_grid();
+        c->bns_grid = bns_persistent_grid(fr.criterion);
         c->raster_grid = raster_fused_grid(fr.PS, o.dice_group);
         c->frame_grid = frame_kernel_grid(fr.PS, o.dice_group);
         launch_clear(c->fb, c->fr, 1, c->stream);
@@ -893,7 +899,7 @@ mp_status mp_finish(mp_ctx* c) {
         c->stats.bounds = (long long)(hc(c, kQTail) >> 32);
         c->stats.passes = 1;
         // reset, clear, (bound-and-split, dice+raster | one overlapped kernel), exact slow raster, resolve
-        c->stats.kernels = c->opt.overlap ? 5 : 6;
+        c->stats.kernels = overlapped(c) ? 5 : 6;
     } else {
         CK(cudaEventRecord(c->ev1, c->stream));
         st = read_ctrl(c);

@@ -70,7 +70,7 @@ void launch_bns_reset(unsigned long long* ctrl, long long roots, cudaStream_t s)
 void launch_bns_persistent(const DrawDev* draws, const int* root_prefix, int n_draws, const FrameDev& fr,
                            const Queue& q, const SubPatches& out, unsigned long long* ctrl, int grid,
                            long long spin_limit, cudaStream_t s);
-int bns_persistent_grid();
+int bns_persistent_grid(int criterion);
 // plain per-pass bound-and-split (the reference's BOUNDED structure)
 void launch_bns_init_stack(const Queue& stack, int draw, int n_patches, cudaStream_t s);
 void launch_bns_pass(const DrawDev* draws, const FrameDev& fr, const Queue& stack, long long offset, int batch,

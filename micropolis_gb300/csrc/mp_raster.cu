@@ -462,7 +462,8 @@ __global__ void __launch_bounds__(kFusedThreads, 3)
                 reinterpret_cast<int*>(sd)[i] = __ldg(reinterpret_cast<const int*>(gdraws) + i);
             __syncthreads();
         }
-        bns_warp_loop(staged ? sd : gdraws, root_prefix, n_draws, fr, q, sub, sub.seq, ctrl, spin_limit);
+        // the CPU criterion only: the host runs the GPU criterion as two launches
+        bns_warp_loop<0>(staged ? sd : gdraws, root_prefix, n_draws, fr, q, sub, sub.seq, ctrl, spin_limit);
         __syncthreads();
     }
     SM& sm = *reinterpret_cast<SM*>(smem_raw);

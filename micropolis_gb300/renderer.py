@@ -74,6 +74,7 @@ class Renderer:
         o.bns_blocks = int(opts.bns_blocks)
         o.raster_tile = int(opts.raster_tile)
         o.dice_group = int(opts.dice_group)
+        o.bound_criterion = int(opts.bound_criterion)
         self._ctx = ctypes.c_void_p()
         st = lib().mp_create(ctypes.byref(o), ctypes.byref(self._ctx))
         if st != 0:

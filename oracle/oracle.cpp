@@ -209,9 +209,17 @@ static void bound_range(const PatchRange& r, const float* cp, int type, const fl
     }
 }
 
+// The reference's GPU criterion (kernels/bound_n_split.h), defined with the
+// kernel restatement below.
+enum GpuBound { kGpuCull = 0, kGpuDraw = 1, kGpuHSplit = 2, kGpuVSplit = 6 };
+static int bound_gpu(const or_params* P, const or_draw* d, const PatchRange& r);
+
 // src/Reyes/BoundNSplitCLCPU.cpp:31-56 (init) and 75-159 (the LIFO loop).
 // Batches of reyes_patches_per_pass only cut the emission sequence into
-// passes; the sequence itself does not depend on the batch size.
+// passes; the sequence itself does not depend on the batch size.  With the
+// GPU criterion the same loop applies kernels/bound_n_split.h's decision
+// (the emitted set does not depend on the traversal order; VSPLIT halves x,
+// HSPLIT halves y, kernels/bound_n_split_multipass.cl:111-125).
 template <typename Emit>
 static int64_t bound_n_split(const or_params* P, const or_draw* d, Emit emit) {
     Projection proj;
@@ -225,6 +233,22 @@ static int64_t bound_n_split(const or_params* P, const or_draw* d, Emit emit) {
     while (!stack.empty()) {
         PatchRange r = stack.back();
         stack.pop_back();
+        if (P->bound_criterion == 1) {
+            ++bounds;
+            const int g = bound_gpu(P, d, r);
+            if (g == kGpuDraw) {
+                emit(r);
+            } else if (g == kGpuHSplit) {
+                float cy = (r.miny + r.maxy) * 0.5f;
+                stack.push_back(PatchRange{r.minx, r.miny, r.maxx, cy, r.depth + 1, r.patch_id});
+                stack.push_back(PatchRange{r.minx, cy, r.maxx, r.maxy, r.depth + 1, r.patch_id});
+            } else if (g == kGpuVSplit) {
+                float cx = (r.minx + r.maxx) * 0.5f;
+                stack.push_back(PatchRange{r.minx, r.miny, cx, r.maxy, r.depth + 1, r.patch_id});
+                stack.push_back(PatchRange{cx, r.miny, r.maxx, r.maxy, r.depth + 1, r.patch_id});
+            }
+            continue;
+        }
         bound_range(r, d->cp, d->type, d->mv, box, vlen, hlen);
         ++bounds;
         V2 size;
@@ -419,6 +443,70 @@ static void perspective(float fovy_rad, float aspect, float zn, float zf, float*
     m[10] = -(zf + zn) / (zf - zn);
     m[11] = -1.0f;
     m[14] = -(2.0f * zf * zn) / (zf - zn);
+}
+
+// kernels/bound_n_split.h:8-100 -- the reference's GPU bound criterion for
+// one range, in the kernel arithmetic (R1-R6): 3x3 samples at
+// mix(rmin, rmax, (u, v) / 2) through the kernel patch evaluation and the
+// modelview, an eye-space bbox with fmin/fmax, screen positions
+// screen_matrix * (p.xy / p.w) with screen_matrix = diag(W/2, H/2)
+// (Projection.cpp:42-45), outside_frustum with far = 1000
+// (Projection.h:49), the eye-plane split rule, then <= on the larger of the
+// summed screen distances along u (h) and v (v).
+static int bound_gpu(const or_params* P, const or_draw* d, const PatchRange& r) {
+    if (r.depth >= (int64_t)P->max_split_depth - 1) return kGpuCull;
+    const int W = P->width, H = P->height;
+    const float aspect = float(W) / H;
+    float proj[16];
+    perspective((float)(P->fovy_deg * M_PI / 180), aspect, P->near_plane, 10000.0f, proj);
+    Projection pr;
+    pr.init(P->fovy_deg, P->near_plane, W, H, P->cull_ribbon);
+    const float inf = std::numeric_limits<float>::infinity();
+    V3 mn{inf, inf, inf}, mx{-inf, -inf, -inf};
+    V2 pp[3][3];
+    const int ncp = d->type == 0 ? 16 : 20;
+    const float* cp = d->cp + (int64_t)r.patch_id * 3 * ncp;
+    for (int u = 0; u < 3; ++u)
+        for (int v = 0; v < 3; ++v) {
+            float tx = std::fma(r.maxx - r.minx, (float)u * 0.5f, r.minx);
+            float ty = std::fma(r.maxy - r.miny, (float)v * 0.5f, r.miny);
+            V4 o = d->type == 0 ? eval_bezier_k(cp, tx, ty) : eval_gregory_k(cp, tx, ty);
+            V4 p = mul_m44v4(d->mv, o);
+            mn = V3{std::fmin(mn.x, p.x), std::fmin(mn.y, p.y), std::fmin(mn.z, p.z)};
+            mx = V3{std::fmax(mx.x, p.x), std::fmax(mx.y, p.y), std::fmax(mx.z, p.z)};
+            V4 q = mul_m44v4(proj, p);
+            float rw = 1.0f / q.w;
+            float x = q.x * rw, y = q.y * rw;
+            pp[v][u] = V2{std::fma(0.0f, y, pr.vpx * x), std::fma(pr.vpy, y, 0.0f * x)};
+        }
+    // outside_frustum
+    float n = -mx.z, f = -mn.z;
+    if (f < P->near_plane || n > 1000.0f) return kGpuCull;
+    n = std::fmax(P->near_plane, n);
+    float sminx = std::fma(kdiv(mn.x, mn.x < 0 ? n : f), pr.fx, pr.vpx);
+    float sminy = std::fma(kdiv(mn.y, mn.y < 0 ? n : f), pr.fy, pr.vpy);
+    float smaxx = std::fma(kdiv(mx.x, mx.x > 0 ? n : f), pr.fx, pr.vpx);
+    float smaxy = std::fma(kdiv(mx.y, mx.y > 0 ? n : f), pr.fy, pr.vpy);
+    if (sminx > (float)(W - 1) + P->cull_ribbon || smaxx < -P->cull_ribbon ||
+        sminy > (float)(H - 1) + P->cull_ribbon || smaxy < -P->cull_ribbon)
+        return kGpuCull;
+    // eps = P->near * 0.1 with a double literal
+    const float eps = (float)((double)P->near_plane * 0.1);
+    if (mn.z < eps && mx.z > P->near_plane) return (r.maxx - r.minx) < (r.maxy - r.miny) ? kGpuVSplit : kGpuHSplit;
+    float hlen = 0, vlen = 0;
+    for (int i = 0; i < 3; ++i) {
+        float h = 0, v = 0;
+        for (int j = 0; j < 2; ++j) {
+            float hx = pp[i][j].x - pp[i][j + 1].x, hy = pp[i][j].y - pp[i][j + 1].y;
+            float vx = pp[j][i].x - pp[j + 1][i].x, vy = pp[j][i].y - pp[j + 1][i].y;
+            h += std::sqrt(std::fma(hy, hy, hx * hx));
+            v += std::sqrt(std::fma(vy, vy, vx * vx));
+        }
+        hlen = std::fmax(h, hlen);
+        vlen = std::fmax(v, vlen);
+    }
+    if (hlen <= P->bound_n_split_limit && vlen <= P->bound_n_split_limit) return kGpuDraw;
+    return hlen > vlen ? kGpuVSplit : kGpuHSplit;
 }
 
 struct Frame {

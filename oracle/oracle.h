@@ -53,6 +53,8 @@ typedef struct {
     int32_t displacement;
     float displacement_amplitude;   /* multiplies the 0.04/0.02/0.01 amplitudes */
     float clear_color[4];
+    int32_t bound_criterion;        /* 0: CPU criterion (BoundNSplitCLCPU.cpp), 1: GPU criterion
+                                       (kernels/bound_n_split.h), restated with R1-R6 */
 } or_params;
 
 /* CPU bound-and-split of one draw.  Writes the emitted sub-patches in the

@@ -33,7 +33,8 @@ class OrParams(ctypes.Structure):
                 ("max_split_depth", ctypes.c_int32), ("reyes_patches_per_pass", ctypes.c_int32),
                 ("reyes_patch_size", ctypes.c_int32), ("subpixel_bits", ctypes.c_int32),
                 ("backface_culling", ctypes.c_int32), ("displacement", ctypes.c_int32),
-                ("displacement_amplitude", ctypes.c_float), ("clear_color", ctypes.c_float * 4)]
+                ("displacement_amplitude", ctypes.c_float), ("clear_color", ctypes.c_float * 4),
+                ("bound_criterion", ctypes.c_int32)]
 
 
 def build() -> None:
@@ -88,7 +89,7 @@ def _ptr(a, t):
 def make_params(scene, **over) -> OrParams:
     o = dict(bound_n_split_limit=8.0, cull_ribbon=32.0, max_split_depth=23, reyes_patches_per_pass=100000,
              reyes_patch_size=8, subpixel_bits=6, backface_culling=1, displacement=0,
-             displacement_amplitude=1.0, clear_color=(0.1, 0.1, 0.7, 0.0))
+             displacement_amplitude=1.0, clear_color=(0.1, 0.1, 0.7, 0.0), bound_criterion=0)
     o.update({k: v for k, v in scene.options.items() if k in o})
     o.update(over)
     p = OrParams()
@@ -97,7 +98,7 @@ def make_params(scene, **over) -> OrParams:
     for k in ("bound_n_split_limit", "cull_ribbon", "displacement_amplitude"):
         setattr(p, k, float(o[k]))
     for k in ("max_split_depth", "reyes_patches_per_pass", "reyes_patch_size", "subpixel_bits",
-              "backface_culling", "displacement"):
+              "backface_culling", "displacement", "bound_criterion"):
         setattr(p, k, int(o[k]))
     for i in range(4):
         p.clear_color[i] = o["clear_color"][i]

@@ -109,3 +109,32 @@ def test_options_file_and_cli():
     assert o.reyes_patch_size == 16 and o.bound_n_split_limit == 4.0
     assert o.clear_color == (0.0, 0.0, 0.0, 1.0)
     assert o.max_split_depth == 12 and o.backface_culling is False
+
+
+def test_gpu_criterion_oracle_properties(built):
+    """The restated GPU criterion emits dyadic ranges that never overlap
+    within a patch, differs from the CPU criterion, and drops ranges at
+    depth >= max_split_depth - 1."""
+    from micropolis_gb300 import scenes
+    from oracle import oracle
+    sc = scenes.mixed4096_1920x1080(n=128, width=512, height=512)
+    for depth in (23, 6):
+        p = oracle.make_params(sc, bound_criterion=1, max_split_depth=depth)
+        pid, rng, nb = oracle.bound_n_split(sc, 0, params=p)
+        assert len(pid) > 0
+        w = rng[:, 2] - rng[:, 0]
+        h = rng[:, 3] - rng[:, 1]
+        assert np.all(np.frexp(w)[0] == 0.5) and np.all(np.frexp(h)[0] == 0.5)
+        assert np.all(np.mod(rng[:, 0], w) == 0) and np.all(np.mod(rng[:, 1], h) == 0)
+        # splits below the cull depth only: at most depth - 2 halvings
+        assert np.all(-np.log2(w) - np.log2(h) <= depth - 2)
+        for q in np.unique(pid)[:20]:
+            a = rng[pid == q]
+            for i in range(len(a)):
+                for j in range(i + 1, len(a)):
+                    ox = min(a[i, 2], a[j, 2]) - max(a[i, 0], a[j, 0])
+                    oy = min(a[i, 3], a[j, 3]) - max(a[i, 1], a[j, 1])
+                    assert ox <= 0 or oy <= 0
+    cpu_pid, _, _ = oracle.bound_n_split(sc, 0, params=oracle.make_params(sc))
+    gpu_pid, _, _ = oracle.bound_n_split(sc, 0, params=oracle.make_params(sc, bound_criterion=1))
+    assert len(cpu_pid) != len(gpu_pid)
