@@ -230,6 +230,36 @@ mp_status mp_read_image(mp_ctx* ctx, int32_t view, uint8_t* rgb);
  * cap bytes including the terminating zero; MP_ERR_OVERFLOW when truncated. */
 mp_status mp_dump_stats(mp_ctx* ctx, char* buf, size_t cap);
 
+/* ---- .mscene scene files (src/micropolis/mscene.capnp, Scene.cpp:89-197) ----
+ * A scene read from the reference's Cap'n Proto packed file: meshes (name,
+ * patch type, xyz positions), objects (name, mesh, transform, colour),
+ * cameras (name, transform, near, far, fovy) and the number of lights.
+ * Host memory only; no CUDA call. */
+typedef struct mp_scene mp_scene;
+/* Reads and decodes a packed .mscene file (Scene::Scene, Scene.cpp:89-173);
+ * MP_ERR_INVALID_ARG for a file that is not a well-formed scene. */
+mp_status mp_scene_load(const char* path, mp_scene** out);
+/* The same from bytes in memory. */
+mp_status mp_scene_parse(const uint8_t* data, size_t size, mp_scene** out);
+void mp_scene_free(mp_scene* scene);
+mp_status mp_scene_counts(const mp_scene* scene, int32_t* meshes, int32_t* objects, int32_t* cameras,
+                          int32_t* lights);
+/* Mesh i: its name, mp_patch_type and the flattened positions (3 floats per
+ * point, 16 or 20 points per patch); pointers stay valid until mp_scene_free. */
+mp_status mp_scene_mesh(const mp_scene* scene, int32_t i, const char** name, int32_t* type, const float** xyz,
+                        int64_t* n_floats);
+/* Object i: name, mesh index (-1 when no mesh has its mesh name), the
+ * column-major matrix translate(t) * mat4_cast(rotation), colour (rgb, 1). */
+mp_status mp_scene_object(const mp_scene* scene, int32_t i, const char** name, int32_t* mesh, float matrix[16],
+                          float color[4]);
+mp_status mp_scene_camera(const mp_scene* scene, int32_t i, const char** name, float matrix[16], float* near_plane,
+                          float* far_plane, float* fovy_deg);
+/* inverse(camera matrix) * object matrix (Scene.cpp:190). */
+mp_status mp_scene_modelview(const mp_scene* scene, int32_t camera, int32_t object, float mv[16]);
+/* Scene::draw (Scene.cpp:179-197) with camera `camera`: prepare, load each
+ * object's mesh on first use (handle = the mesh), draw every object, finish. */
+mp_status mp_scene_draw(mp_ctx* ctx, const mp_scene* scene, int32_t camera);
+
 /* 64-bit atomicMin throughput probe (atomics per second): pattern 0 uniform
  * random slots, pattern 1 micropolygon-like locality. */
 mp_status mp_atomic_bench(mp_ctx* ctx, int64_t n_slots, int64_t n_ops, int32_t pattern, double* atomics_per_s);

@@ -80,6 +80,15 @@ SIGNATURES = [
     ("mp_atomic_bench", ctypes.c_int, [c_void_p, i64, i64, i32, P(ctypes.c_double)]),
     ("mp_read_image", ctypes.c_int, [c_void_p, i32, P(ctypes.c_uint8)]),
     ("mp_dump_stats", ctypes.c_int, [c_void_p, ctypes.c_char_p, ctypes.c_size_t]),
+    ("mp_scene_load", ctypes.c_int, [ctypes.c_char_p, P(c_void_p)]),
+    ("mp_scene_parse", ctypes.c_int, [ctypes.c_char_p, ctypes.c_size_t, P(c_void_p)]),
+    ("mp_scene_free", None, [c_void_p]),
+    ("mp_scene_counts", ctypes.c_int, [c_void_p, P(i32), P(i32), P(i32), P(i32)]),
+    ("mp_scene_mesh", ctypes.c_int, [c_void_p, i32, P(ctypes.c_char_p), P(i32), P(P(f32)), P(i64)]),
+    ("mp_scene_object", ctypes.c_int, [c_void_p, i32, P(ctypes.c_char_p), P(i32), P(f32), P(f32)]),
+    ("mp_scene_camera", ctypes.c_int, [c_void_p, i32, P(ctypes.c_char_p), P(f32), P(f32), P(f32), P(f32)]),
+    ("mp_scene_modelview", ctypes.c_int, [c_void_p, i32, i32, P(f32)]),
+    ("mp_scene_draw", ctypes.c_int, [c_void_p, c_void_p, i32]),
 ]
 
 _lib = None
