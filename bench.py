@@ -131,8 +131,9 @@ def _cpu_chunk(args):
     from micropolis_gb300 import scenes
     from oracle import oracle
     sc = scenes.WORKLOADS[name]()
-    for d, (a, b) in zip(sc.draws, draw_slices):
-        d.mesh = scenes.Mesh(d.mesh.type, d.mesh.cp[a:b])
+    for d, sl in zip(sc.draws, draw_slices):
+        # (first, end) patch range, or (first, end, stride) for an interleaved share
+        d.mesh = scenes.Mesh(d.mesh.type, d.mesh.cp[slice(*sl)])
     t = time.perf_counter()
     _, _, st = oracle.render(sc)
     return st["micropolygons"], time.perf_counter() - t
@@ -141,8 +142,8 @@ def _cpu_chunk(args):
 def cpu_baseline(name: str, procs: int, patches_per_proc: int, pool=None):
     """micropolygons/s of the oracle path on `procs` processes, each rendering
     its own slice of every draw's patches (a bounded sample); with
-    patches_per_proc = 0 the processes share one frame (process p renders the
-    p-th of `procs` equal parts of every draw).  Returns (rate,
+    patches_per_proc = 0 the processes share one frame (process p renders
+    every procs-th patch of every draw, starting at patch p).  Returns (rate,
     micropolygons, wall s, busiest process s)."""
     from micropolis_gb300 import scenes
     sc = scenes.WORKLOADS[name]()
@@ -152,7 +153,7 @@ def cpu_baseline(name: str, procs: int, patches_per_proc: int, pool=None):
         for d in sc.draws:
             n = d.mesh.n_patches
             if patches_per_proc <= 0:
-                sl.append((n * p // procs, n * (p + 1) // procs))
+                sl.append((p, n, procs))    # every procs-th patch: the shares cost about the same
                 continue
             share = max(1, patches_per_proc // len(sc.draws))
             a = (p * share) % max(1, n)
