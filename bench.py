@@ -113,6 +113,24 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
+def max_over_ranks(x: float, device=None) -> float:
+    """The largest value of x over the ranks of the process group (x itself
+    when there is no group): the whole job is as slow as its slowest rank."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return x
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_rate(units_per_rank: float, seconds_max: float, world: int) -> float:
+    """Whole-job throughput of `world` independent replicas (weak scaling):
+    the units all ranks processed over the slowest rank's time."""
+    return units_per_rank * world / seconds_max
+
+
 def measured_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -370,14 +388,10 @@ def main():
         t_wall = time.perf_counter() - t_wall
         torch.cuda.nvtx.range_pop()
     frame_ms = [a.elapsed_time(b) for a, b in evs]
-    t_dev = sum(frame_ms) / 1e3
+    t_dev = max_over_ranks(sum(frame_ms) / 1e3, dev)
     if world > 1:
-        t = torch.tensor([t_dev], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        t_dev = float(t.item())
         torch.distributed.barrier()
-    total_mp = mpoly * args.steps * world
-    value = total_mp / t_dev
+    value = replica_rate(mpoly * args.steps, t_dev, world)
     stats = r.stats()
     _, depth_now = r.read_framebuffer()
     covered = int(np.count_nonzero(depth_now != 0x7FFFFFFF))
@@ -411,7 +425,7 @@ def main():
         t = time.perf_counter()
         e2e_step()
         e2e_times.append(time.perf_counter() - t)
-    e2e_value = mpoly / statistics.mean(e2e_times) * world
+    e2e_value = replica_rate(mpoly * args.steps, max_over_ranks(sum(e2e_times), dev), world)
 
     # ---- stage timing pass (same frame, stages as separate launches)
     r.set_stage_timing(True)
