@@ -50,6 +50,7 @@ __global__ void __launch_bounds__(kBnsBlock) bns_persistent_kernel(const DrawDev
                                                                    long long spin_limit) {
     // draw constants staged in shared memory when they fit
     __shared__ DrawDev s_draws[kBnsSmemDraws];
+    __shared__ float s_pts[27 * kBnsBlock];   // nine bound samples per thread
     const bool staged = n_draws <= kBnsSmemDraws;
     if (staged) {
         const int words = n_draws * (int)(sizeof(DrawDev) / 4);
@@ -57,7 +58,8 @@ __global__ void __launch_bounds__(kBnsBlock) bns_persistent_kernel(const DrawDev
             reinterpret_cast<int*>(s_draws)[i] = __ldg(reinterpret_cast<const int*>(gdraws) + i);
         __syncthreads();
     }
-    bns_warp_loop<CRIT>(staged ? s_draws : gdraws, root_prefix, n_draws, fr, q, out, nullptr, ctrl, spin_limit);
+    bns_warp_loop<CRIT, CRIT == 0 ? kBnsBlock : 0>(staged ? s_draws : gdraws, root_prefix, n_draws, fr, q, out, nullptr,
+                                                   ctrl, spin_limit, s_pts);
 }
 
 // ---------------------------------------------------------------------------

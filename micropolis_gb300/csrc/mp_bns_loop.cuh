@@ -46,10 +46,18 @@ constexpr unsigned long long kNoTicket = ~0ull;
 // raised.  Emitted sub-patches go to `out`; when out_seq is given, each
 // emitted slot is also marked with the frame's epoch (release) for consumers
 // that run concurrently.  CRIT selects the bound criterion (bns_decide).
-template <int CRIT>
+// With the CPU criterion and ST > 0 (the block's thread count), children take
+// six of their nine bound samples from the parent through the queue's pts
+// records (which must exist); `pts` is shared memory of 27 floats per thread
+// (point layout of spi()).
+template <int CRIT, int ST>
 __device__ __forceinline__ void bns_warp_loop(const DrawDev* draws, const int* __restrict__ root_prefix, int n_draws,
                                               const FrameDev& fr, const Queue& q, const SubPatches& out,
-                                              unsigned* out_seq, unsigned long long* ctrl, long long spin_limit) {
+                                              unsigned* out_seq, unsigned long long* ctrl, long long spin_limit,
+                                              float* pts) {
+    constexpr bool inherit = CRIT == 0 && ST > 0;
+    constexpr int st = ST;
+    float* sp = inherit ? pts + threadIdx.x : nullptr;
     const int lane = threadIdx.x & 31;
     const unsigned epoch = (unsigned)*(volatile unsigned long long*)cw(ctrl, kEpoch);
     const unsigned long long R = *(volatile unsigned long long*)cw(ctrl, kRoots);
@@ -96,6 +104,7 @@ __device__ __forceinline__ void bns_warp_loop(const DrawDev* draws, const int* _
         int pid = 0, draw = 0, depth = 0;
         int dec = -1;
         if (ready) {
+            int flag = kInheritNone;
             if (ticket < R) {
                 // root: find the draw whose patch range holds this ticket
                 int lo = 0, hi = n_draws - 1;
@@ -112,8 +121,12 @@ __device__ __forceinline__ void bns_warp_loop(const DrawDev* draws, const int* _
                 pid = (int)m.x;
                 draw = (int)(m.y & 0xffffffu);
                 depth = (int)(m.y >> 24);
+                if (inherit) flag = load_inherited(q.pts + slot * kPtsPerSlot, sp, st);
             }
-            dec = bns_decide<CRIT>(draws[draw], fr, pid, r, depth);
+            if (inherit)
+                dec = bns_decide_inherit(draws[draw], fr, pid, r, depth, flag, sp, st);
+            else
+                dec = bns_decide<CRIT>(draws[draw], fr, pid, r, depth);
         }
         // One lane issues the step's three independent atomics back to back,
         // so their round trips overlap: output slots for emitted sub-patches,
@@ -158,6 +171,10 @@ __device__ __forceinline__ void bns_warp_loop(const DrawDev* draws, const int* _
                 q.range[s0 + 1] = c1;
                 q.meta[s0] = make_uint2((unsigned)pid, meta_y);
                 q.meta[s0 + 1] = make_uint2((unsigned)pid, meta_y);
+                if (inherit) {
+                    store_inherited(q.pts + s0 * kPtsPerSlot, dec, 0, depth + 1, sp, st);
+                    store_inherited(q.pts + (s0 + 1) * kPtsPerSlot, dec, 1, depth + 1, sp, st);
+                }
                 // release: the item stores above are visible before the slot's epoch
                 st_release_u32(q.seq + s0, epoch);
                 st_release_u32(q.seq + s0 + 1, epoch);

@@ -172,8 +172,9 @@ __device__ __forceinline__ void bbox_add(RangeBound& b, const F3& p) {
 // order, vlen/hlen take maximum() in index order 0, 1, 2, and the bbox
 // (minimum/maximum that skip NaN) does not depend on the visiting order.
 // Eye-space points of the samples (iu, iv), iu = 0..2, of one column iv of
-// the 3x3 grid.
-__device__ __forceinline__ void bound_column(const DrawDev& d, int pid, float4 r, int iv, F3 cur[3]) {
+// the 3x3 grid; only the samples whose bit is set in `need` are evaluated.
+__device__ __forceinline__ void bound_column(const DrawDev& d, int pid, float4 r, int iv, F3 cur[3],
+                                             unsigned need = 7u) {
     float sv[3];
 #pragma unroll
     for (int i = 0; i < 3; ++i) sv[i] = fadd(r.x, fmul(fmul(fsub(r.z, r.x), (float)i), 0.5f));
@@ -188,11 +189,13 @@ __device__ __forceinline__ void bound_column(const DrawDev& d, int pid, float4 r
             row[i] = spline3(wt, ld3(P + 4 * i + 0), ld3(P + 4 * i + 1), ld3(P + 4 * i + 2), ld3(P + 4 * i + 3));
 #pragma unroll
         for (int iu = 0; iu < 3; ++iu)
-            cur[iu] = mv_point(d.mv, spline3(spline_weights(sv[iu]), row[0], row[1], row[2], row[3]));
+            if (need & (1u << iu))
+                cur[iu] = mv_point(d.mv, spline3(spline_weights(sv[iu]), row[0], row[1], row[2], row[3]));
     } else {
         const float4* P = d.cp + (size_t)pid * 20;
 #pragma unroll
-        for (int iu = 0; iu < 3; ++iu) cur[iu] = mv_point(d.mv, eval_gregory_cpu(P, su_iv, sv[iu]));
+        for (int iu = 0; iu < 3; ++iu)
+            if (need & (1u << iu)) cur[iu] = mv_point(d.mv, eval_gregory_cpu(P, su_iv, sv[iu]));
     }
 }
 
@@ -633,12 +636,147 @@ __device__ __forceinline__ int bns_decide_gpu(const DrawDev& d, const FrameDev& 
     return hlen > vlen ? kSplitX : kSplitY;
 }
 
+// ---------------------------------------------------------------------------
+// Samples inherited from the parent range.  A child of a split shares two of
+// its three sample lines with its parent: splitting x at cx, the low child's
+// sample columns iu = 0, 2 lie at the parent's iu = 0, 1 and the high
+// child's at the parent's iu = 1, 2 (likewise rows iv for a split of y).
+// With dyadic ranges whose sides are multiples of 2^-24 (split depth <= 24)
+// every sample parameter is formed exactly, so the shared samples are the
+// same floats as the parent's and their evaluation would give the same
+// points bit for bit; the child takes them from its queue record and
+// evaluates only the three new ones.
+constexpr int kInheritNone = 0, kInheritX = 1, kInheritY = 2;
+constexpr int kInheritMaxDepth = 24;
+constexpr int kPtsPerSlot = 5;   // float4 per queue record of inherited samples
+
+// Points of a lane's current range in shared memory: point (iu, iv),
+// component c at sp[((3 * iv + iu) * 3 + c) * st].
+__device__ __forceinline__ int spi(int iu, int iv, int c, int st) { return ((3 * iv + iu) * 3 + c) * st; }
+
+// bound_range with the samples that `flag` marks as inherited already in
+// sp; evaluates the others, leaves all nine points in sp and returns the
+// same bound as bound_range.
+__device__ __forceinline__ RangeBound bound_range_inherit(const DrawDev& d, int pid, float4 r, int flag, float* sp,
+                                                          int st) {
+    RangeBound b;
+    const float inf = __int_as_float(0x7f800000);
+    b.bmin = F3{inf, inf, inf};
+    b.bmax = F3{-inf, -inf, -inf};
+    b.vlen = 0.0f;
+    float hsum[3] = {0.0f, 0.0f, 0.0f};
+    F3 prev[3];
+#pragma unroll 1
+    for (int iv = 0; iv < 3; ++iv) {
+        const unsigned need = flag == kInheritX ? 2u : (flag == kInheritY && iv != 1) ? 0u : 7u;
+        F3 cur[3];
+#pragma unroll
+        for (int iu = 0; iu < 3; ++iu)
+            if (!(need & (1u << iu)))
+                cur[iu] = F3{sp[spi(iu, iv, 0, st)], sp[spi(iu, iv, 1, st)], sp[spi(iu, iv, 2, st)]};
+        if (need) bound_column(d, pid, r, iv, cur, need);
+#pragma unroll
+        for (int iu = 0; iu < 3; ++iu)
+            if (need & (1u << iu)) {
+                sp[spi(iu, iv, 0, st)] = cur[iu].x;
+                sp[spi(iu, iv, 1, st)] = cur[iu].y;
+                sp[spi(iu, iv, 2, st)] = cur[iu].z;
+            }
+#pragma unroll
+        for (int iu = 0; iu < 3; ++iu) bbox_add(b, cur[iu]);
+        b.vlen = maximum(column_length(cur), b.vlen);
+        if (iv > 0) {
+#pragma unroll
+            for (int iu = 0; iu < 3; ++iu) hsum[iu] = fadd(hsum[iu], distance3(prev[iu], cur[iu]));
+        }
+#pragma unroll
+        for (int iu = 0; iu < 3; ++iu) prev[iu] = cur[iu];
+    }
+    b.hlen = 0.0f;
+#pragma unroll
+    for (int iu = 0; iu < 3; ++iu) b.hlen = maximum(hsum[iu], b.hlen);
+    return b;
+}
+
+// Queue record of inherited samples (kPtsPerSlot float4): six points, three
+// floats each, in the order the flag implies -- kInheritX: (0, iv), (2, iv)
+// for iv = 0..2; kInheritY: (iu, 0), (iu, 2) for iu = 0..2 -- and the flag
+// in the last float.
+__device__ __forceinline__ void inherited_slot(int flag, int k, int& iu, int& iv) {
+    if (flag == kInheritX) {
+        iu = k < 3 ? 0 : 2;
+        iv = k % 3;
+    } else {
+        iu = k % 3;
+        iv = k < 3 ? 0 : 2;
+    }
+}
+
+// Reads a record into sp; returns its flag.
+__device__ __forceinline__ int load_inherited(const float4* rec, float* sp, int st) {
+    const int flag = __float_as_int(__ldcg(rec + kPtsPerSlot - 1).w);
+    if (flag != kInheritX && flag != kInheritY) return kInheritNone;
+    // float j of the record is component j % 3 of point j / 3
+#pragma unroll
+    for (int k = 0; k < kPtsPerSlot; ++k) {
+        const float4 v = __ldcg(rec + k);
+        const float f[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            const int j = 4 * k + e;
+            if (j < 18) {
+                int iu, iv;
+                inherited_slot(flag, j / 3, iu, iv);
+                sp[spi(iu, iv, j % 3, st)] = f[e];
+            }
+        }
+    }
+    return flag;
+}
+
+// Writes the record of child `half` (0 low, 1 high) of a range split by
+// `dec`, from the parent's nine points in sp; kInheritNone past the depth
+// where sample parameters stay exact.
+__device__ __forceinline__ void store_inherited(float4* rec, int dec, int half, int child_depth, const float* sp,
+                                                int st) {
+    int flag = kInheritNone;
+    if (child_depth <= kInheritMaxDepth && (dec == kSplitX || dec == kSplitY))
+        flag = dec == kSplitX ? kInheritX : kInheritY;
+    if (flag == kInheritNone) {
+        rec[kPtsPerSlot - 1] = make_float4(0.0f, 0.0f, 0.0f, __int_as_float(kInheritNone));
+        return;
+    }
+#pragma unroll
+    for (int k = 0; k < kPtsPerSlot; ++k) {
+        float f[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            const int j = 4 * k + e;
+            if (j < 18) {
+                int iu, iv;
+                inherited_slot(flag, j / 3, iu, iv);
+                // the child's line 0 / 2 is the parent's line half / half + 1
+                if (flag == kInheritX) iu = half + (iu == 2 ? 1 : 0);
+                else iv = half + (iv == 2 ? 1 : 0);
+                f[e] = sp[spi(iu, iv, j % 3, st)];
+            }
+        }
+        if (k == kPtsPerSlot - 1) f[3] = __int_as_float(flag);
+        rec[k] = make_float4(f[0], f[1], f[2], f[3]);
+    }
+}
+
 // The decision of one range.  CRIT: 0 the CPU criterion, 1 the GPU
 // criterion, -1 chosen at run time from fr.criterion (one kernel for both).
 template <int CRIT>
 __device__ __forceinline__ int bns_decide(const DrawDev& d, const FrameDev& fr, int pid, float4 r, int depth) {
     if (CRIT == 1 || (CRIT < 0 && fr.criterion == 1)) return bns_decide_gpu(d, fr, pid, r, depth);
     return bns_decide_bound(d, fr, bound_range(d, pid, r), depth);
+}
+// The CPU criterion with inherited samples (sp as in bound_range_inherit).
+__device__ __forceinline__ int bns_decide_inherit(const DrawDev& d, const FrameDev& fr, int pid, float4 r, int depth,
+                                                  int flag, float* sp, int st) {
+    return bns_decide_bound(d, fr, bound_range_inherit(d, pid, r, flag, sp, st), depth);
 }
 
 }  // namespace mp

@@ -161,10 +161,12 @@ mp_status grow_queue(mp_ctx* c, long long need) {
     cudaFree(c->q.range);
     cudaFree(c->q.meta);
     cudaFree(c->q.seq);
+    cudaFree(c->q.pts);
     c->q = Queue{};
     CK(dalloc(&c->q.range, cap));
     CK(dalloc(&c->q.meta, cap));
     CK(dalloc(&c->q.seq, cap));
+    CK(dalloc(&c->q.pts, cap * kPtsPerSlot));
     CK(cudaMemsetAsync(c->q.seq, 0, sizeof(unsigned) * (size_t)cap, c->stream));
     c->q.capacity = cap;
     return MP_OK;
@@ -712,7 +714,7 @@ void mp_destroy(mp_ctx* c) {
     dfree(c->d_root_prefix);
     if (c->h_draws) cudaFreeHost(c->h_draws);
     if (c->h_root_prefix) cudaFreeHost(c->h_root_prefix);
-    dfree(c->q.range); dfree(c->q.meta); dfree(c->q.seq);
+    dfree(c->q.range); dfree(c->q.meta); dfree(c->q.seq); dfree(c->q.pts);
     dfree(c->sub.range); dfree(c->sub.meta); dfree(c->sub.seq);
     dfree(c->big);
     dfree(c->mshade);
@@ -983,7 +985,8 @@ mp_status mp_dump_stats(mp_ctx* c, char* buf, size_t cap) {
         long long bytes;
     } mem[] = {
         {"control points", cp},
-        {"work queue", c->q.capacity * (long long)(sizeof(float4) + sizeof(uint2) + sizeof(unsigned))},
+        {"work queue", c->q.capacity * (long long)(sizeof(float4) * (1 + kPtsPerSlot) + sizeof(uint2) +
+                                                   sizeof(unsigned))},
         {"sub-patch list", c->sub.capacity * (long long)(sizeof(float4) + sizeof(int2) + sizeof(unsigned))},
         {"diffuse factors", c->mshade_cap * (long long)sizeof(float)},
         {"framebuffer", c->fb.key_pixels * c->fb.views * 8 + c->fb.pixels * c->fb.views * 20},

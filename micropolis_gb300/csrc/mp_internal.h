@@ -35,6 +35,9 @@ struct Queue {              // bound-and-split work queue (structure of arrays)
     float4* range;          // (min.x, min.y, max.x, max.y)
     uint2* meta;            // (patch id, draw | depth << 24)
     unsigned* seq;          // epoch of the frame that wrote the slot
+    // kPtsPerSlot float4 per slot: six of the item's nine bound samples, taken
+    // from its parent, and which three are missing (or nullptr: none kept)
+    float4* pts;
     long long capacity;
 };
 

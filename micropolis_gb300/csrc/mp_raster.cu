@@ -443,13 +443,27 @@ __global__ void __launch_bounds__(kFusedThreads, 3)
 // have the lowest indices, so the blocks that wait never wait on a block that
 // has not started; a wait that runs out stops consumption and reports
 // MP_ERR_TIMEOUT.
+// Shared memory of the frame kernel: the raster's, or what its
+// bound-and-split blocks stage (draw records, nine samples per thread).
+constexpr int kFrameStagedDraws = 64;
+constexpr size_t kFramePtsOffset = (kFrameStagedDraws * sizeof(DrawDev) + 15) / 16 * 16;
+template <int PS, int NS>
+constexpr size_t frame_smem() {
+    return sizeof(FusedSmem<PS, NS>) > kFramePtsOffset + 27 * kFusedThreads * sizeof(float)
+               ? sizeof(FusedSmem<PS, NS>)
+               : kFramePtsOffset + 27 * kFusedThreads * sizeof(float);
+}
+
 template <int PS, int NS>
 __global__ void __launch_bounds__(kFusedThreads, 3)
     frame_kernel(const DrawDev* __restrict__ gdraws, const int* __restrict__ root_prefix, int n_draws, FrameDev fr,
                  Queue q, SubPatches sub, Framebuffer fb, float* __restrict__ mshade, BigQuad* big, long long big_cap,
                  unsigned long long* ctrl, long long spin_limit, int n_bns_ctas) {
     using SM = FusedSmem<PS, NS>;
-    constexpr int kStaged = (int)(sizeof(SM) / sizeof(DrawDev)) < 64 ? (int)(sizeof(SM) / sizeof(DrawDev)) : 64;
+    // bound-and-split blocks: draw records, then the bound samples of each thread
+    // (frame_smem() sizes the launch for both uses)
+    constexpr int kStaged = kFrameStagedDraws;
+    constexpr size_t kPtsOffset = kFramePtsOffset;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ long long s_group;
     if ((int)blockIdx.x < n_bns_ctas) {
@@ -463,7 +477,9 @@ __global__ void __launch_bounds__(kFusedThreads, 3)
             __syncthreads();
         }
         // the CPU criterion only: the host runs the GPU criterion as two launches
-        bns_warp_loop<0>(staged ? sd : gdraws, root_prefix, n_draws, fr, q, sub, sub.seq, ctrl, spin_limit);
+        float* pts = reinterpret_cast<float*>(smem_raw + kPtsOffset);
+        bns_warp_loop<0, kFusedThreads>(staged ? sd : gdraws, root_prefix, n_draws, fr, q, sub, sub.seq, ctrl,
+                                        spin_limit, pts);
         __syncthreads();
     }
     SM& sm = *reinterpret_cast<SM*>(smem_raw);
@@ -852,7 +868,7 @@ int frame_kernel_grid(int PS, int group) {
     int g = 0;
     dispatch_group(PS, group, [&](auto t) {
         using T = decltype(t);
-        g = resident_grid(frame_kernel<T::ps, T::ns>, sizeof(FusedSmem<T::ps, T::ns>));
+        g = resident_grid(frame_kernel<T::ps, T::ns>, frame_smem<T::ps, T::ns>());
     });
     return g;
 }
@@ -863,7 +879,7 @@ void launch_frame_kernel(const DrawDev* draws, const int* root_prefix, int n_dra
                          cudaStream_t s) {
     dispatch_group(fr.PS, group, [&](auto t) {
         using T = decltype(t);
-        frame_kernel<T::ps, T::ns><<<grid, kFusedThreads, sizeof(FusedSmem<T::ps, T::ns>), s>>>(
+        frame_kernel<T::ps, T::ns><<<grid, kFusedThreads, frame_smem<T::ps, T::ns>(), s>>>(
             draws, root_prefix, n_draws, fr, q, sub, fb, mshade, big, big_cap, ctrl, spin_limit, n_bns_ctas);
     });
 }

@@ -421,11 +421,6 @@ void mul(const float a[16], const float b[16], float out[16]) {
         }
 }
 
-mp_status fail(mp_scene* s, const char* msg) {
-    if (s) s->err = msg;
-    return MP_ERR_INVALID_ARG;
-}
-
 }  // namespace
 
 extern "C" {

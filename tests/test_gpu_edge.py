@@ -152,3 +152,39 @@ def test_many_views_batched_equals_per_view_plain(built, cuda):
         assert bad <= COVERAGE_BUDGET * zb.size
         rp.close()
     rb.close()
+
+
+def test_no_draws(built, cuda):
+    """prepare + finish with nothing drawn leaves the cleared frame."""
+    from micropolis_gb300 import scenes
+    from micropolis_gb300.renderer import renderer_for
+    sc = _small_scene()
+    for path in ("batched", "plain"):
+        r = renderer_for(sc, path)
+        r.prepare()
+        r.finish()
+        assert r.stats()["subpatches"] == 0 and r.stats()["fragments"] == 0
+        col, dep = r.read_framebuffer()
+        assert np.all(dep == 0x7FFFFFFF)
+        r.close()
+
+
+def test_more_draws_than_staged(built, cuda):
+    """100 draws (beyond the 64 draw records staged in shared memory), each a
+    few patches of its own mesh, in both paths."""
+    from micropolis_gb300 import scenes
+    base = _small_scene(n=200)
+    draws = []
+    for k in range(100):
+        d = base.draws[k % 2]
+        draws.append(scenes.Draw(scenes.Mesh(d.mesh.type, d.mesh.cp[2 * (k // 2):2 * (k // 2) + 2].copy()), d.mv,
+                                 d.color))
+    sc = scenes.Scene("many", base.width, base.height, draws, options=dict(base.options))
+    for path in ("batched", "plain"):
+        _check(sc, path)
+
+
+def test_largest_frame(built, cuda):
+    """A 4096-pixel-wide frame (the fast raster's coordinate bound at 6 subpixel bits)."""
+    sc = _small_scene(n=64, width=4096, height=2304)
+    _check(sc, "batched")
