@@ -88,6 +88,10 @@ struct mp_ctx {
     int graph_draws = -1;
     long long graph_roots = -1;
     const void* graph_key[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    // set by every reallocation of a buffer the graph's kernels use: a new
+    // allocation may land at the freed one's address, so the pointers above
+    // cannot tell that the captured sizes and pointers are stale
+    bool graph_stale = false;
 
     int bns_grid = 0, raster_grid = 0, frame_grid = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -152,11 +156,12 @@ void perspective(float fovy_rad, float aspect, float zn, float zf, float* m) {
 }
 
 // first-frame guesses; both grow (and the frame is rendered again) on overflow
-long long auto_queue_cap(long long roots) { return std::min(std::max(1LL << 22, roots * 128), 1LL << 28); }
+long long auto_queue_cap(long long roots) { return std::min(std::max(1LL << 22, roots * 32), 1LL << 28); }
 long long auto_sub_cap(long long roots) { return std::min(std::max(1LL << 21, roots * 64), 1LL << 26); }
 
 mp_status grow_queue(mp_ctx* c, long long need) {
     if (need <= c->q.capacity) return MP_OK;
+    c->graph_stale = true;
     long long cap = std::max(need, c->q.capacity * 2);
     cudaFree(c->q.range);
     cudaFree(c->q.meta);
@@ -176,6 +181,7 @@ mp_status grow_sub(mp_ctx* c, long long need, bool keep) {
     const long long id_limit = (long long)(0xffffffffull / ((unsigned long long)c->fr.PS * c->fr.PS));
     if (need > id_limit) return fail(c, MP_ERR_OVERFLOW, "frame exceeds the 32-bit micropolygon id range");
     if (need <= c->sub.capacity) return MP_OK;
+    c->graph_stale = true;
     long long cap = std::min(std::max(need, c->sub.capacity * 2), id_limit);
     SubPatches n{};
     CK(dalloc(&n.range, cap));
@@ -199,6 +205,7 @@ mp_status grow_sub(mp_ctx* c, long long need, bool keep) {
 
 mp_status grow_big(mp_ctx* c, long long need) {
     if (need <= c->big_cap) return MP_OK;
+    c->graph_stale = true;
     long long cap = std::max(need, c->big_cap * 2);
     cudaFree(c->big);
     c->big = nullptr;
@@ -210,6 +217,7 @@ mp_status grow_big(mp_ctx* c, long long need) {
 mp_status ensure_mshade(mp_ctx* c) {
     const long long need = c->sub.capacity * c->fr.PS * c->fr.PS;
     if (need <= c->mshade_cap) return MP_OK;
+    c->graph_stale = true;
     dfree(c->mshade);
     c->mshade = nullptr;
     c->mshade_cap = 0;
@@ -220,6 +228,7 @@ mp_status ensure_mshade(mp_ctx* c) {
 
 mp_status ensure_draws(mp_ctx* c, int n) {
     if (n <= c->draws_cap) return MP_OK;
+    c->graph_stale = true;
     int cap = std::max(n, std::max(4, c->draws_cap * 2));
     // earlier draws of a plain frame may still be read by queued kernels: keep them
     CK(cudaStreamSynchronize(c->stream));
@@ -437,6 +446,7 @@ mp_status capture_frame(mp_ctx* c, int n, long long roots) {
     if (e != cudaSuccess) return cuda_fail(c, e, "cudaGraphInstantiate");
     c->graph_draws = n;
     c->graph_roots = roots;
+    c->graph_stale = false;
     c->graph_key[0] = c->q.range;
     c->graph_key[1] = c->sub.range;
     c->graph_key[2] = c->big;
@@ -509,9 +519,9 @@ mp_status batched_frame(mp_ctx* c) {
                 prev = c->sev[k];
             }
         } else {
-        if (!c->graph || c->graph_draws != n || c->graph_roots != roots || c->graph_key[0] != c->q.range ||
-            c->graph_key[1] != c->sub.range || c->graph_key[2] != c->big || c->graph_key[3] != c->d_draws ||
-            c->graph_key[4] != c->mshade) {
+        if (!c->graph || c->graph_stale || c->graph_draws != n || c->graph_roots != roots ||
+            c->graph_key[0] != c->q.range || c->graph_key[1] != c->sub.range || c->graph_key[2] != c->big ||
+            c->graph_key[3] != c->d_draws || c->graph_key[4] != c->mshade) {
             st = capture_frame(c, n, roots);
             if (st) return st;
         }
@@ -533,7 +543,14 @@ mp_status batched_frame(mp_ctx* c) {
         if (outc > c->sub.capacity && ((st = grow_sub(c, outc + outc / 4, false)) || (st = ensure_mshade(c))))
             return st;
         if (bigc > c->big_cap && (st = grow_big(c, bigc * 2))) return st;
-        if (attempt == 7) return fail(c, MP_ERR_OVERFLOW, "capacity still exceeded after regrowth");
+        if (attempt == 7) {
+            char msg[256];
+            std::snprintf(msg, sizeof(msg),
+                          "capacity still exceeded after regrowth (queue %lld/%lld, sub-patches %lld/%lld, "
+                          "slow quads %lld/%lld)",
+                          pushed, c->q.capacity, outc, c->sub.capacity, bigc, c->big_cap);
+            return fail(c, MP_ERR_OVERFLOW, msg);
+        }
     }
     return MP_OK;
 }

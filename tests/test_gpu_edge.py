@@ -188,3 +188,20 @@ def test_largest_frame(built, cuda):
     """A 4096-pixel-wide frame (the fast raster's coordinate bound at 6 subpixel bits)."""
     sc = _small_scene(n=64, width=4096, height=2304)
     _check(sc, "batched")
+
+
+def test_regrowth_over_many_frames(built, cuda):
+    """Frames whose buffers regrow between renders (first frame from small
+    capacities, then a larger scene in the same context) keep matching the
+    oracle: the captured frame graph is rebuilt after every reallocation."""
+    from micropolis_gb300.renderer import render_scene, renderer_for
+    small = _small_scene(n=64)
+    big = _small_scene(n=512)
+    r = renderer_for(small, "batched", queue_capacity=64, subpatch_capacity=16)
+    for sc in (small, big, small, big):
+        render_scene(r, sc)
+        want, ocol, odep, ost = _oracle(sc)
+        d, p, g = r.subpatches()
+        assert subpatch_set(p, g, d) == want
+        assert r.stats()["fragments"] == ost["fragments"]
+    r.close()
