@@ -41,7 +41,7 @@ L2_FLUSH_BYTES = 256 << 20
 # profiles/bns_persistent_mixed4096_1920x1080.md and
 # profiles/resolve_mixed4096_1920x1080.md).  ncu replays with cold
 # caches, so these are upper bounds for a launch inside a frame.
-NCU_TRAFFIC = {"dice_raster": 102_631_936 + 65_886_976, "bound_split": 2_533_120 + 27_202_816,
+NCU_TRAFFIC = {"dice_raster": 102_915_072 + 67_311_104, "bound_split": 2_964_480 + 201_067_776,
                "resolve_or_shade": 62_764_032 + 8_419_328}
 
 
@@ -460,7 +460,7 @@ def main():
     # key clear, 8 B key + 16 B colour + 4 B depth per pixel for the resolve.
     cp_alg = sum(d.mesh.n_patches * d.mesh.cp.shape[1] * 12 for d in sc.draws)
     alg = {"dice_raster": cp_alg + S * 20,
-           "bound_split": cp_alg + S * 20,
+           "bound_split": cp_alg + S * 20 + stats["bounds"] * (28 + 80),
            "resolve_or_shade": W * H * (8 + 16 + 4),
            "clear": W * H * 8,
            "raster_big": 0}
