@@ -43,6 +43,10 @@ L2_FLUSH_BYTES = 256 << 20
 # caches, so these are upper bounds for a launch inside a frame.
 NCU_TRAFFIC = {"dice_raster": 102_915_072 + 67_311_104, "bound_split": 2_964_480 + 201_067_776,
                "resolve_or_shade": 62_764_032 + 8_419_328}
+# Warp instructions per launch (smsp__inst_executed.sum) from the same
+# captures: the dice+raster kernel is bound by instruction issue, whose peak
+# is 4 warp instructions per SM per cycle.
+NCU_INST = {"dice_raster": 1_254_612_573, "bound_split": 170_754_545}
 
 
 def parse():
@@ -481,6 +485,14 @@ def main():
                           "frac_hbm": frame_bytes / frame_s / 1e9 / peak_gbs,
                           "frac_atomic": frags / frame_s / atom_peak["tiled"] if atom_peak["tiled"] else None},
                 "note": "dice+raster is issue-bound (FP32/ALU instruction issue), not HBM- or atomic-bound"}
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    clk = clk.summary()
+    mhz = clk.get("sm_mhz") or clk.get("sm_max_mhz") or 0
+    if dominant in NCU_INST and mhz and dom_s > 0:
+        peak_issue = sms * 4 * mhz * 1e6
+        roofline["issue"] = {"kernel": dominant, "achieved": NCU_INST[dominant] / dom_s, "peak": peak_issue,
+                             "unit": "warp instructions/s", "frac": NCU_INST[dominant] / dom_s / peak_issue,
+                             "sms": sms, "sm_mhz": mhz}
 
     extras = {}
     if not args.no_extras and rank == 0:
@@ -548,7 +560,7 @@ def main():
                         "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * statistics.mean(e2e_times)},
                 "gpu_launches": stats["kernels"] * args.steps,
                 "roofline": roofline,
-                "clocks": clk.summary()}
+                "clocks": clk}
         if "cpu_baseline" in extras:
             line["cpu_baseline"] = extras.pop("cpu_baseline")
         line.update(extras)

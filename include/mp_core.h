@@ -151,6 +151,18 @@ mp_status mp_draw_patches(mp_ctx* ctx, uint64_t handle, const float modelview[16
 /* Same, into framebuffer layer `view` (batched independent views). */
 mp_status mp_draw_patches_view(mp_ctx* ctx, uint64_t handle, const float modelview[16], const mp_projection* proj,
                                const float color[4], int32_t view);
+
+/* One draw of a batch: mesh handle, modelview, projection, colour, layer. */
+typedef struct {
+    uint64_t handle;
+    float modelview[16];
+    mp_projection proj;
+    float color[4];
+    int32_t view;
+} mp_view;
+/* n draws at once (mp_draw_patches_view for each, in order); stops at the
+ * first error and returns it. */
+mp_status mp_draw_views(mp_ctx* ctx, int32_t n, const mp_view* views);
 /* Renderer::finish (RendererCL.cpp:138-154): completes the frame; the framebuffer
  * is ready when this returns. */
 mp_status mp_finish(mp_ctx* ctx);

@@ -37,6 +37,11 @@ class MpProjection(ctypes.Structure):
     _fields_ = [("fovy_deg", ctypes.c_float), ("near_plane", ctypes.c_float), ("viewport", ctypes.c_int32 * 2)]
 
 
+class MpView(ctypes.Structure):
+    _fields_ = [("handle", ctypes.c_uint64), ("modelview", ctypes.c_float * 16), ("proj", MpProjection),
+                ("color", ctypes.c_float * 4), ("view", ctypes.c_int32)]
+
+
 class MpStats(ctypes.Structure):
     _fields_ = [("subpatches", ctypes.c_int64), ("micropolygons", ctypes.c_int64), ("bounds", ctypes.c_int64),
                 ("passes", ctypes.c_int64), ("fragments", ctypes.c_int64), ("big_quads", ctypes.c_int64),
@@ -61,6 +66,7 @@ SIGNATURES = [
     ("mp_prepare", ctypes.c_int, [c_void_p]),
     ("mp_draw_patches", ctypes.c_int, [c_void_p, u64, P(f32), P(MpProjection), P(f32)]),
     ("mp_draw_patches_view", ctypes.c_int, [c_void_p, u64, P(f32), P(MpProjection), P(f32), i32]),
+    ("mp_draw_views", ctypes.c_int, [c_void_p, i32, P(MpView)]),
     ("mp_finish", ctypes.c_int, [c_void_p]),
     ("mp_set_stage_timing", ctypes.c_int, [c_void_p, i32]),
     ("mp_dump_trace", ctypes.c_int, [c_void_p, ctypes.c_char_p, ctypes.c_size_t]),

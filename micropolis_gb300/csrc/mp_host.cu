@@ -901,6 +901,16 @@ mp_status mp_draw_patches_view(mp_ctx* c, uint64_t handle, const float mv[16], c
     return MP_OK;
 }
 
+mp_status mp_draw_views(mp_ctx* c, int32_t n, const mp_view* views) {
+    if (!c || n < 0 || (n > 0 && !views)) return MP_ERR_INVALID_ARG;
+    for (int32_t i = 0; i < n; ++i) {
+        const mp_view& v = views[i];
+        mp_status st = mp_draw_patches_view(c, v.handle, v.modelview, &v.proj, v.color, v.view);
+        if (st) return st;
+    }
+    return MP_OK;
+}
+
 mp_status mp_draw_patches(mp_ctx* c, uint64_t handle, const float mv[16], const mp_projection* proj,
                           const float color[4]) {
     return mp_draw_patches_view(c, handle, mv, proj, color, 0);

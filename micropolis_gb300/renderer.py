@@ -132,6 +132,17 @@ class Renderer:
         p = projection.c()
         self._ck(lib().mp_draw_patches_view(self._ctx, handle, _f32p(mv), ctypes.byref(p), _f32p(col), view))
 
+    def draw_views(self, items) -> None:
+        """Many draws in one call: items of (handle, modelview, projection, colour, view)."""
+        arr = (_lib.MpView * max(1, len(items)))()
+        for k, (h, mv, proj, col, view) in enumerate(items):
+            arr[k].handle = h
+            arr[k].modelview[:] = [float(x) for x in np.asarray(mv, np.float32).reshape(16)]
+            arr[k].proj = proj.c()
+            arr[k].color[:] = [float(x) for x in np.asarray(col, np.float32).reshape(4)]
+            arr[k].view = int(view)
+        self._ck(lib().mp_draw_views(self._ctx, len(items), arr))
+
     def _text(self, fn) -> str:
         size = 4096
         while True:

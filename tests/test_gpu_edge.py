@@ -205,3 +205,32 @@ def test_regrowth_over_many_frames(built, cuda):
         assert subpatch_set(p, g, d) == want
         assert r.stats()["fragments"] == ost["fragments"]
     r.close()
+
+
+def test_draw_views_equals_per_draw_calls(built, cuda):
+    """mp_draw_views (a batch of draws in one call) renders the frame that the
+    same draws issued one by one render."""
+    from micropolis_gb300 import scenes
+    from micropolis_gb300.renderer import Projection, renderer_for
+    sc = scenes.views64_512x512(n_views=4, size=256)
+    for d in sc.draws:
+        d.mesh = scenes.Mesh(d.mesh.type, d.mesh.cp[:200])
+    proj = Projection(sc.fovy, sc.near, (sc.width, sc.height))
+    frames = []
+    for batch in (False, True):
+        r = renderer_for(sc, "batched")
+        for k, d in enumerate(sc.draws):
+            r.load_patches(10 + k, d.mesh.cp, d.mesh.type)
+        r.prepare()
+        if batch:
+            r.draw_views([(10 + k, d.mv, proj, d.color, d.view) for k, d in enumerate(sc.draws)])
+        else:
+            for k, d in enumerate(sc.draws):
+                r.draw_patches(10 + k, d.mv, proj, d.color, view=d.view)
+        r.finish()
+        d_, p_, g_ = r.subpatches()
+        frames.append((subpatch_set(p_, g_, d_), [r.read_framebuffer(view=v)[1] for v in range(4)]))
+        r.close()
+    assert frames[0][0] == frames[1][0]
+    for a, b in zip(frames[0][1], frames[1][1]):
+        assert np.array_equal(a, b)
