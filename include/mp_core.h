@@ -269,7 +269,8 @@ mp_status mp_scene_camera(const mp_scene* scene, int32_t i, const char** name, f
 /* inverse(camera matrix) * object matrix (Scene.cpp:190). */
 mp_status mp_scene_modelview(const mp_scene* scene, int32_t camera, int32_t object, float mv[16]);
 /* Scene::draw (Scene.cpp:179-197) with camera `camera`: prepare, load each
- * object's mesh on first use (handle = the mesh), draw every object, finish. */
+ * object's mesh on first use (one handle per mesh of this scene), draw every
+ * object, finish. */
 mp_status mp_scene_draw(mp_ctx* ctx, const mp_scene* scene, int32_t camera);
 
 /* 64-bit atomicMin throughput probe (atomics per second): pattern 0 uniform

@@ -25,6 +25,7 @@
 //   Mesh        ptr0 name, ptr1 positions (List(Float32)); u16 #0 type
 //   Transform   ptr0 translation, ptr1 rotation
 //   Vec3        f32 #0 x, #1 y, #2 z;  Quaternion f32 #0 r, #1 i, #2 j, #3 k
+#include <atomic>
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
@@ -59,6 +60,7 @@ struct mp_scene {
     std::vector<Camera> cameras;
     int32_t lights = 0;
     std::string err;
+    uint64_t uid = 0;   // distinct for every scene read in this process
 };
 
 namespace {
@@ -443,7 +445,9 @@ mp_status mp_scene_parse(const uint8_t* data, size_t size, mp_scene** out) {
     *out = nullptr;
     Message m;
     if (!unpack(data, size, m.w) || !parse_frame(m)) return MP_ERR_INVALID_ARG;
+    static std::atomic<uint64_t> next_uid{1};
     mp_scene* s = new mp_scene();
+    s->uid = next_uid.fetch_add(1);
     if (!decode(m, *s)) {
         delete s;
         return MP_ERR_INVALID_ARG;
@@ -531,8 +535,10 @@ mp_status mp_scene_draw(mp_ctx* ctx, const mp_scene* s, int32_t camera) {
         const auto& o = s->objects[i];
         if (o.mesh < 0) continue;   // an unknown mesh name draws nothing
         const auto& m = s->meshes[(size_t)o.mesh];
-        // the mesh's address is its handle, as the reference uses Mesh* (Scene.cpp:186)
-        const uint64_t handle = (uint64_t)(uintptr_t)&m;
+        // one handle per mesh, as the reference keys on Mesh* (Scene.cpp:186); built
+        // from the scene's process-wide id rather than an address, so that a
+        // later scene whose mesh lands at a freed one's address is loaded anew
+        const uint64_t handle = (s->uid << 32) | (uint64_t)(uint32_t)o.mesh;
         int32_t loaded = 0;
         if ((st = mp_are_patches_loaded(ctx, handle, &loaded))) return st;
         if (!loaded && (st = mp_load_patches(ctx, handle, m.xyz.data(), m.xyz.size() / 3,
