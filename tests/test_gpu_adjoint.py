@@ -74,3 +74,34 @@ def test_adjoint_bwd_cost(built, cuda):
     from micropolis_gb300 import adjoint
     res = adjoint.bench_bwd_fwd(steps=5)
     assert res["bwd_over_fwd"] <= 2.5, res
+
+
+def test_adjoint_gregory_matches_fp64(built, cuda):
+    """The same check on the heightfield turned into Gregory patches (the
+    20-point layout of tools/bez2mscene_greg.py), through the face blends."""
+    torch = cuda
+    from micropolis_gb300 import adjoint, scenes
+    from oracle import oracle
+    sc = scenes.heightfield16_512x512()
+    d = sc.draws[0]
+    d.mesh = scenes.Mesh(scenes.GREGORY, np.ascontiguousarray(d.mesh.cp[:, scenes.BEZIER_TO_GREGORY, :]))
+    dr = adjoint.DiffRenderer(sc)
+    dev = torch.device("cuda")
+    cp0 = torch.tensor(d.mesh.cp, device=dev)
+    rng = np.random.default_rng(sc.seed + 200)
+    cpt = cp0 + torch.tensor(rng.normal(0, 0.05, size=cp0.shape).astype(np.float32), device=dev)
+    target = dr.render(cpt, 1.2).clone()
+    cp = cp0.clone().requires_grad_(True)
+    amp = torch.tensor(1.0, device="cuda", requires_grad=True)
+    img = adjoint.render(cp, amp, dr)
+    loss = ((img - target) ** 2).sum()
+    loss.backward()
+    torch.cuda.synchronize()
+    win = dr.r.visibility(0)
+    _, pid, rng_ = dr.r.subpatches()
+    cpd = cp0.double().cpu().numpy()
+    L, g_ref, ga_ref = oracle.loss_fp64(sc, pid, rng_, win, target.cpu().numpy(), cpd, 1.0)
+    assert abs(L - float(loss.detach())) <= 1e-4 * abs(L)
+    g_gpu = cp.grad.double().cpu().numpy()
+    assert np.linalg.norm(g_gpu - g_ref) <= GRAD_RTOL * np.linalg.norm(g_ref)
+    assert abs(float(amp.grad) - ga_ref) <= GRAD_RTOL * abs(ga_ref)
