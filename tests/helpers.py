@@ -17,3 +17,23 @@ def framebuffer_diff(color_a, depth_a, color_b, depth_b, rel=1e-5):
     dbad = np.asarray(depth_a) != np.asarray(depth_b)
     exact = np.any(ca != cb, axis=1) | dbad
     return int(np.count_nonzero(cbad | dbad)), int(np.count_nonzero(exact))
+
+
+GOLDEN_DIR = __import__("os").path.join(__import__("os").path.dirname(__import__("os").path.abspath(__file__)),
+                                        "golden")
+GOLDEN_CASES = ("heightfield_1024x768", "mixed96_bezier_512", "mixed96_gregory_512", "mixed96_gregory_depth3_512",
+                "heightfield_eye_plane_512x384")
+
+
+def golden_case(name):
+    """(scene, options, pid, range) of a golden fixture written by
+    tests/golden/make_golden.py from the reference's own bound-and-split."""
+    import os
+    from micropolis_gb300 import scenes
+    z = np.load(os.path.join(GOLDEN_DIR, name + ".npz"))
+    opts = dict(bound_n_split_limit=float(z["limit"]), cull_ribbon=float(z["cull_ribbon"]),
+                max_split_depth=int(z["max_split_depth"]))
+    draw = scenes.Draw(scenes.Mesh(int(z["type"]), z["cp"].copy()), z["mv"].copy(), (0.9, 0.7, 0.3, 1.0))
+    sc = scenes.Scene(name, int(z["width"]), int(z["height"]), [draw], fovy=float(z["fovy"]), near=float(z["near"]),
+                      options=dict(opts))
+    return sc, opts, z["pid"], z["range"]

@@ -1,0 +1,22 @@
+"""Both CUDA paths against the golden vectors of the reference's own CPU
+bound-and-split (tests/golden/): the emitted sub-patch set, bit for bit."""
+import numpy as np
+import pytest
+
+from helpers import GOLDEN_CASES, golden_case, subpatch_set
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("path", ["batched", "plain"])
+@pytest.mark.parametrize("name", GOLDEN_CASES)
+def test_cuda_matches_golden(built, cuda, name, path):
+    from micropolis_gb300.renderer import render_scene, renderer_for
+    sc, opts, gpid, grng = golden_case(name)
+    r = renderer_for(sc, path, **opts)
+    render_scene(r, sc)
+    d, pid, rng = r.subpatches()
+    got = subpatch_set(pid, rng, d)
+    assert len(got) == len(pid) == len(gpid)
+    assert got == subpatch_set(gpid, grng, np.zeros(len(gpid), np.int32))
+    r.close()
