@@ -1,16 +1,36 @@
 #!/bin/sh
 # Compiles the reference's own src/base/Patch.cpp and src/base/Projection.cpp
 # from the reference tree (read in place, never copied) together with the pin
-# driver ref_pin.cpp into oracle/_ref/libref_pin.so.  The reference's other
+# driver ref_pin.cpp, and the reference's kernels (rewritten for C++ into
+# oracle/_ref/kernels/, outside the repository's history) with the CPU
+# work-item runtime ref_kernels.cpp, into oracle/_ref/libref_pin.so.  The reference's other
 # sources need OpenCL, OpenGL, GLFW, boost, capnp and generated config headers
 # and are not compiled.  Skips quietly when the reference tree is absent.
+#
+# The CPU sources compile without floating-point contraction (the reference's
+# CPU build on x86 has none).  The kernels compile with contraction on, as
+# OpenCL C compiles them (FP_CONTRACT defaults to ON); x86 needs -mfma for
+# gcc to emit fused multiply-adds, Arm has them in its base instruction set.
 set -e
 HERE=$(cd "$(dirname "$0")" && pwd)
 REF=${MP_REFERENCE_DIR:-/root/reference}
 [ -f "$REF/src/base/Patch.cpp" ] || { echo "build_ref: no reference tree at $REF, skipped"; exit 0; }
-mkdir -p "$HERE/_ref"
-g++ -std=c++14 -O2 -ffp-contract=off -fno-fast-math -fPIC -shared -w \
-    -I "$HERE/refshim" -I "$REF/src/base" \
-    "$REF/src/base/Patch.cpp" "$REF/src/base/Projection.cpp" "$HERE/ref_pin.cpp" \
-    -o "$HERE/_ref/libref_pin.so"
-echo "build_ref: $HERE/_ref/libref_pin.so"
+OUT="$HERE/_ref"
+mkdir -p "$OUT/obj"
+FMA=
+case $(uname -m) in x86_64|amd64) FMA=-mfma ;; esac
+COMMON="-std=c++17 -O2 -fno-fast-math -fwrapv -fPIC -w -pthread"
+PIDS=
+for f in "$REF/src/base/Patch.cpp" "$REF/src/base/Projection.cpp" "$HERE/ref_pin.cpp"; do
+    g++ $COMMON -ffp-contract=off -I "$HERE/refshim" -I "$REF/src/base" -I "$HERE" -c "$f" \
+        -o "$OUT/obj/$(basename "$f" .cpp).o" &
+    PIDS="$PIDS $!"
+done
+# The reference's kernels (kernels/*.cl) rewritten into C++ by clshim/rewrite.py,
+# into _ref/kernels/ only, then compiled with the fiber runtime ref_kernels.cpp.
+python3 "$HERE/clshim/rewrite.py" "$REF/kernels" "$OUT/kernels"
+g++ $COMMON $FMA -ffp-contract=fast -I "$HERE" -c "$HERE/ref_kernels.cpp" -o "$OUT/obj/ref_kernels.o"
+for p in $PIDS; do wait "$p"; done
+g++ -shared -pthread "$OUT/obj/Patch.o" "$OUT/obj/Projection.o" "$OUT/obj/ref_pin.o" "$OUT/obj/ref_kernels.o" \
+    -o "$OUT/libref_pin.so"
+echo "build_ref: $OUT/libref_pin.so"

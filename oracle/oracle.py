@@ -314,3 +314,38 @@ def parse_stats(text):
         v = v.strip()
         out[k.strip()] = [int(t) for t in v.split()] if k.strip() == "bound_n_split_balance" else int(v)
     return out
+
+
+def ref_render(scene, params=None, threads=None):
+    """The reference's own kernels (kernels/*.cl compiled as C++ by
+    oracle/build_ref.sh) after its CPU bound-and-split: (tiled colour
+    float32[W*H,4], tiled depth int32[W*H], sub-patch count), or None where
+    the reference tree was not compiled."""
+    L = ref_pin()
+    if L is None or not hasattr(L, "refk_render"):
+        return None
+    p = params or make_params(scene)
+    n = len(scene.draws)
+    cps = [np.ascontiguousarray(d.mesh.cp, np.float32).reshape(-1) for d in scene.draws]
+    cp_ptrs = (f32p * max(1, n))(*[_ptr(c, f32p) for c in cps])
+    npatch = np.array([d.mesh.n_patches for d in scene.draws], np.int32)
+    types = np.array([d.mesh.type for d in scene.draws], np.int32)
+    mvs = np.ascontiguousarray(np.stack([np.asarray(d.mv, np.float32) for d in scene.draws]).reshape(-1))
+    cols = np.ascontiguousarray(np.stack([np.asarray(d.color, np.float32) for d in scene.draws]).reshape(-1))
+    clear = np.asarray(list(p.clear_color), np.float32)
+    npx = scene.width * scene.height
+    color = np.zeros((npx, 4), np.float32)
+    depth = np.zeros(npx, np.int32)
+    L.refk_render.restype = ctypes.c_long
+    L.refk_render.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                              ctypes.c_float, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                              ctypes.c_int, f32p, ctypes.c_int, ctypes.POINTER(f32p), i32p, i32p, f32p, f32p, f32p,
+                              i32p, ctypes.c_int]
+    s = L.refk_render(scene.width, scene.height, p.fovy_deg, p.near_plane, p.cull_ribbon, p.bound_n_split_limit,
+                      p.max_split_depth, p.reyes_patches_per_pass, p.reyes_patch_size, p.subpixel_bits,
+                      p.backface_culling, p.displacement, _ptr(clear, f32p), n, cp_ptrs, _ptr(npatch, i32p),
+                      _ptr(types, i32p), _ptr(mvs, f32p), _ptr(cols, f32p), _ptr(color, f32p), _ptr(depth, i32p),
+                      int(threads or os.cpu_count() or 1))
+    if s < 0:
+        raise ValueError("reference render failed")
+    return color, depth, int(s)

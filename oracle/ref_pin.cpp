@@ -46,6 +46,16 @@ int refpin_projection_bound(float fovy, float near_plane, int w, int h, float ri
     return cull ? 1 : 0;
 }
 
+// Projection::calc_projection (src/base/Projection.cpp:37-40): the glm
+// perspective matrix the reference's dice kernel gets, column major.
+void refpin_projection_matrix(float fovy, float near_plane, int w, int h, float* out16) {
+    Reyes::Projection projection(fovy, near_plane, ivec2(w, h));
+    mat4 proj;
+    projection.calc_projection(proj);
+    for (int c = 0; c < 4; ++c)
+        for (int r = 0; r < 4; ++r) out16[4 * c + r] = proj[c][r];
+}
+
 // The LIFO loop of src/Reyes/BoundNSplitCLCPU.cpp:75-159 and the range bound
 // of :249-336, written over the reference's eval_patch / eval_gregory_patch,
 // BBox, maximum and Projection::bound.
