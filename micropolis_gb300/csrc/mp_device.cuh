@@ -620,10 +620,13 @@ __device__ __forceinline__ int bns_decide_gpu(const DrawDev& d, const FrameDev& 
     const float f = -mnz;
     if (f < d.near_plane || n > 1000.0f) return kCull;
     n = fmaxf(d.near_plane, n);
-    const float sminx = ffma(kdiv(mnx, mnx < 0 ? n : f), d.fx, d.vpx);
-    const float sminy = ffma(kdiv(mny, mny < 0 ? n : f), d.fy, d.vpy);
-    const float smaxx = ffma(kdiv(mxx, mxx > 0 ? n : f), d.fx, d.vpx);
-    const float smaxy = ffma(kdiv(mxy, mxy > 0 ? n : f), d.fy, d.vpy);
+    // `x / n * f.x + screen_size.x * 0.5`: the 0.5 is a double literal, so the
+    // product is rounded to float before a double addition of W/2, which is
+    // exact, then rounded to float: one float multiply and one float add.
+    const float sminx = fadd(fmul(kdiv(mnx, mnx < 0 ? n : f), d.fx), d.vpx);
+    const float sminy = fadd(fmul(kdiv(mny, mny < 0 ? n : f), d.fy), d.vpy);
+    const float smaxx = fadd(fmul(kdiv(mxx, mxx > 0 ? n : f), d.fx), d.vpx);
+    const float smaxy = fadd(fmul(kdiv(mxy, mxy > 0 ? n : f), d.fy), d.vpy);
     if (sminx > fadd((float)(d.vx - 1), d.cull_ribbon) || smaxx < -d.cull_ribbon ||
         sminy > fadd((float)(d.vy - 1), d.cull_ribbon) || smaxy < -d.cull_ribbon)
         return kCull;

@@ -3,9 +3,10 @@
 // INFRASTRUCTURE ONLY.  Vectors are unions of their components and read-only
 // swizzle views (v.xyz converts to a float3), component-wise operators,
 // comparisons giving -1 / 0 masks, and the work-item functions of the
-// fiber runtime in ref_kernels.cpp.  Arithmetic is plain IEEE float (the
-// reference builds with -cl-fast-relaxed-math -cl-mad-enable, which leaves
-// rounding open; comparisons against the oracle are tolerance-based).
+// fiber runtime in ref_kernels.cpp.  Arithmetic is IEEE float with the
+// floating-point contraction of the build (the reference builds with
+// -cl-fast-relaxed-math -cl-mad-enable, which leaves rounding open;
+// comparisons against the oracle allow for it).
 #pragma once
 #include <cmath>
 #include <cstddef>
@@ -43,6 +44,8 @@ struct Swz16 {
     inline T& operator+=(T& a, T b) { a = a + b; return a; }                                    \
     inline T& operator-=(T& a, T b) { a = a - b; return a; }                                    \
     inline T& operator*=(T& a, T b) { a = a * b; return a; }
+
+typedef unsigned char uchar;
 
 struct float2;
 struct float3;
@@ -170,6 +173,10 @@ inline float max(float a, float b) { return std::fmax(a, b); }
 inline float min(float a, float b) { return std::fmin(a, b); }
 inline int max(int a, int b) { return a > b ? a : b; }
 inline int min(int a, int b) { return a < b ? a : b; }
+inline float3 min(float3 a, float3 b) { return float3(min(a.x, b.x), min(a.y, b.y), min(a.z, b.z)); }
+inline float3 max(float3 a, float3 b) { return float3(max(a.x, b.x), max(a.y, b.y), max(a.z, b.z)); }
+inline float dot(float2 a, float2 b) { return a.x * b.x + a.y * b.y; }
+inline float distance(float2 a, float2 b) { return std::sqrt(dot(a - b, a - b)); }
 inline int2 max(int2 a, int2 b) { return int2(max(a.x, b.x), max(a.y, b.y)); }
 inline int2 min(int2 a, int2 b) { return int2(min(a.x, b.x), min(a.y, b.y)); }
 inline float clamp(float x, float a, float b) { return std::fmin(std::fmax(x, a), b); }

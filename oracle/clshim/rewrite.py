@@ -1,5 +1,5 @@
 """Rewrites the reference's OpenCL C kernels (kernels/utility.h, dice.cl,
-reyes.cl, framebuffer.cl) into C++ that compiles over cl_shim.h, into
+reyes.cl, framebuffer.cl, bound_n_split.h) into C++ that compiles over cl_shim.h, into
 oracle/_ref/kernels/ (never into the repository): TEST INFRASTRUCTURE ONLY.
 
 Only what C++ cannot express through the shim is rewritten:
@@ -17,7 +17,7 @@ import os
 import re
 import sys
 
-FILES = ("utility.h", "dice.cl", "reyes.cl", "framebuffer.cl")
+FILES = ("utility.h", "dice.cl", "reyes.cl", "framebuffer.cl", "bound_n_split.h")
 
 
 def rewrite(text: str) -> str:

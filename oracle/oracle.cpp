@@ -483,10 +483,13 @@ static int bound_gpu(const or_params* P, const or_draw* d, const PatchRange& r) 
     float n = -mx.z, f = -mn.z;
     if (f < P->near_plane || n > 1000.0f) return kGpuCull;
     n = std::fmax(P->near_plane, n);
-    float sminx = std::fma(kdiv(mn.x, mn.x < 0 ? n : f), pr.fx, pr.vpx);
-    float sminy = std::fma(kdiv(mn.y, mn.y < 0 ? n : f), pr.fy, pr.vpy);
-    float smaxx = std::fma(kdiv(mx.x, mx.x > 0 ? n : f), pr.fx, pr.vpx);
-    float smaxy = std::fma(kdiv(mx.y, mx.y > 0 ? n : f), pr.fy, pr.vpy);
+    // x / n * f.x + screen_size.x * 0.5 with a double literal: the float
+    // product is rounded, then W/2 is added exactly in double and the sum
+    // rounded to float -- the same as one float addition.
+    float sminx = (float)((double)(kdiv(mn.x, mn.x < 0 ? n : f) * pr.fx) + P->width * 0.5);
+    float sminy = (float)((double)(kdiv(mn.y, mn.y < 0 ? n : f) * pr.fy) + P->height * 0.5);
+    float smaxx = (float)((double)(kdiv(mx.x, mx.x > 0 ? n : f) * pr.fx) + P->width * 0.5);
+    float smaxy = (float)((double)(kdiv(mx.y, mx.y > 0 ? n : f) * pr.fy) + P->height * 0.5);
     if (sminx > (float)(W - 1) + P->cull_ribbon || smaxx < -P->cull_ribbon ||
         sminy > (float)(H - 1) + P->cull_ribbon || smaxy < -P->cull_ribbon)
         return kGpuCull;

@@ -266,6 +266,33 @@ def ref_bound_n_split(scene, draw_index=0, params=None):
     return pid[:n], rng[:n]
 
 
+def ref_bound_n_split_gpu(scene, draw_index=0, params=None):
+    """The reference's GPU bound criterion (kernels/bound_n_split.h compiled
+    as C++ by oracle/build_ref.sh) over one draw: (pid int32[S], range
+    float32[S,4]) as a set in LIFO order, or None where the reference tree
+    was not compiled."""
+    L = ref_pin()
+    if L is None or not hasattr(L, "refk_bound_n_split_gpu"):
+        return None
+    p = params or make_params(scene)
+    d = scene.draws[draw_index]
+    cp = np.ascontiguousarray(d.mesh.cp, np.float32).reshape(-1)
+    mv = np.ascontiguousarray(d.mv, np.float32)
+    f = L.refk_bound_n_split_gpu
+    f.restype = ctypes.c_long
+    f.argtypes = [f32p, ctypes.c_int, ctypes.c_int, f32p, ctypes.c_float, ctypes.c_float, ctypes.c_int, ctypes.c_int,
+                  ctypes.c_float, ctypes.c_float, ctypes.c_int, i32p, f32p, ctypes.c_long]
+    args = (_ptr(cp, f32p), d.mesh.n_patches, d.mesh.type, _ptr(mv, f32p), p.fovy_deg, p.near_plane, p.width,
+            p.height, p.cull_ribbon, p.bound_n_split_limit, p.max_split_depth)
+    n = f(*args, None, None, 0)
+    if n < 0:
+        raise ValueError("reference bound-and-split ran past its range budget")
+    pid = np.zeros(max(n, 1), np.int32)
+    rng = np.zeros((max(n, 1), 4), np.float32)
+    f(*args, _ptr(pid, i32p), _ptr(rng, f32p), n)
+    return pid[:n], rng[:n]
+
+
 def display_image(color_tiled, width, height, tile=8):
     """The image the reference's tex_draw shader shows (shaders/tex_draw.frag):
     pixel (x, y) of the framebuffer is texel (gx + ceil(W/tile) * gy) * tile^2

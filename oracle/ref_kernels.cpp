@@ -21,10 +21,13 @@
 
 #include "clshim/cl_shim.h"
 
-// The reference's compile-time constants (RendererCL.cpp:73-87), run-time here.
+// The reference's compile-time constants (RendererCL.cpp:73-87 and
+// BoundNSplitCLBounded.cpp:61-62), run-time here.
 struct RefkConfig {
     int patch_size = 8, tile_size = 8, pxl_shift = 6, backface = 1, displacement = 0;
     int2 grid_size, vp_min_px, vp_max_px, vp_size_px, fb_size;
+    float cull_ribbon = 32.0f;
+    int max_split_depth = 22;
 };
 static RefkConfig g_cfg;
 #define PATCH_SIZE (g_cfg.patch_size)
@@ -37,6 +40,9 @@ static RefkConfig g_cfg;
 #define BACKFACE_CULLING (g_cfg.backface)
 #define PXLCOORD_SHIFT (g_cfg.pxl_shift)
 #define DISPLACEMENT (g_cfg.displacement)
+#define CULL_RIBBON (g_cfg.cull_ribbon)
+#define MAX_SPLIT_DEPTH (g_cfg.max_split_depth)
+#define BOUND_SAMPLE_RATE 3   // reyes.options bound_sample_rate (src/Reyes/config.xml:92)
 
 // ---------------------------------------------------------------------------
 // fiber runtime
@@ -155,6 +161,16 @@ namespace refk_gregory {
 #include "_ref/kernels/dice.inc"
 #undef eval_patch
 }
+namespace refk_bound_bezier {
+#define eval_patch eval_bezier_patch
+#include "_ref/kernels/bound_n_split.h"
+#undef eval_patch
+}
+namespace refk_bound_gregory {
+#define eval_patch eval_gregory_patch
+#include "_ref/kernels/bound_n_split.h"
+#undef eval_patch
+}
 
 // ---------------------------------------------------------------------------
 // frame driver
@@ -164,6 +180,67 @@ long refpin_bound_n_split(const float* cp_in, int n_patches, int type, const flo
                           float near_plane, int w, int h, float ribbon, float limit, int max_split_depth, int* pid,
                           float* range, long cap);
 void refpin_projection_matrix(float fovy, float near_plane, int w, int h, float* out16);
+void refpin_screen_params(float fovy, float near_plane, int w, int h, float* f2, float* vp2);
+
+// The reference's GPU bound-and-split for one draw: bound() of
+// kernels/bound_n_split.h:42-100 per range, with the projection record of
+// init_projection_buffer (BoundNSplitCLBounded.cpp:108-121), the split of
+// the move kernel (kernels/bound_n_split_multipass.cl:103-128: children at
+// depth + 1 around c = (rmin + rmax) * 0.5f) and DRAW ranges emitted, over a
+// LIFO stack.  The emitted set does not depend on the order of visits.
+// Writes at most cap records; returns the count, or -1 past 2^26 ranges.
+long refk_bound_n_split_gpu(const float* cp_in, int n_patches, int type, const float* mv16, float fovy,
+                            float near_plane, int w, int h, float ribbon, float limit, int max_split_depth, int* pid,
+                            float* range, long cap) {
+    g_cfg.cull_ribbon = ribbon;
+    g_cfg.max_split_depth = max_split_depth;
+    const int per = type == 0 ? 16 : 20;
+    std::vector<float4> patch((size_t)n_patches * per);
+    for (size_t k = 0; k < patch.size(); ++k)
+        patch[k] = float4(cp_in[3 * k], cp_in[3 * k + 1], cp_in[3 * k + 2], 1.0f);
+    float proj16[16], f2[2], vp2[2];
+    refpin_projection_matrix(fovy, near_plane, w, h, proj16);
+    refpin_screen_params(fovy, near_plane, w, h, f2, vp2);
+    projection P;
+    for (int c = 0; c < 4; ++c) P.proj.m[c] = float4(proj16[4 * c], proj16[4 * c + 1], proj16[4 * c + 2], proj16[4 * c + 3]);
+    P.screen_matrix.m[0] = float2(vp2[0], 0.0f);
+    P.screen_matrix.m[1] = float2(0.0f, vp2[1]);
+    P.fovy = fovy;
+    P.f = float2(f2[0], f2[1]);
+    P.near = near_plane;
+    P.far = 1000.0f;   // Projection::far() (src/base/Projection.h:49)
+    P.screen_size = int2(w, h);
+    matrix4 mv;
+    for (int c = 0; c < 4; ++c) mv.m[c] = float4(mv16[4 * c], mv16[4 * c + 1], mv16[4 * c + 2], mv16[4 * c + 3]);
+    struct R { int pid; uchar depth; float2 mn, mx; };
+    std::vector<R> stack;
+    for (int i = n_patches - 1; i >= 0; --i) stack.push_back(R{i, 0, float2(0, 0), float2(1, 1)});
+    long n = 0, visits = 0;
+    while (!stack.empty()) {
+        R r = stack.back();
+        stack.pop_back();
+        if (++visits > (1L << 26)) return -1;
+        const uchar flag = type == 0
+            ? refk_bound_bezier::bound(patch.data(), r.pid, r.mn, r.mx, r.depth, &mv, &P, limit)
+            : refk_bound_gregory::bound(patch.data(), r.pid, r.mn, r.mx, r.depth, &mv, &P, limit);
+        if (flag & 1) {
+            if (n < cap) {
+                pid[n] = r.pid;
+                range[4 * n] = r.mn.x; range[4 * n + 1] = r.mn.y;
+                range[4 * n + 2] = r.mx.x; range[4 * n + 3] = r.mx.y;
+            }
+            ++n;
+        } else if (flag & 2) {
+            const float2 c = (r.mn + r.mx) * 0.5f;
+            R a{r.pid, (uchar)(r.depth + 1), r.mn, r.mx}, b{r.pid, (uchar)(r.depth + 1), r.mn, r.mx};
+            if (flag & 4) { a.mx = float2(c.x, r.mx.y); b.mn = float2(c.x, r.mn.y); }
+            else { a.mx = float2(r.mx.x, c.y); b.mn = float2(r.mn.x, c.y); }
+            stack.push_back(b);
+            stack.push_back(a);
+        }
+    }
+    return n;
+}
 
 // One frame as RendererCL draws it: clear (kernels/framebuffer.cl and the
 // depth fill of RendererCL.cpp:115-135), then per draw the reference's CPU

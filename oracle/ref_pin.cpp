@@ -56,6 +56,19 @@ void refpin_projection_matrix(float fovy, float near_plane, int w, int h, float*
         for (int r = 0; r < 4; ++r) out16[4 * c + r] = proj[c][r];
 }
 
+// Projection::f() and the diagonal of Projection::calc_screen_matrix
+// (src/base/Projection.cpp:47-50): what init_projection_buffer stores for the
+// reference's GPU bound criterion besides the projection matrix.
+void refpin_screen_params(float fovy, float near_plane, int w, int h, float* f2, float* vp2) {
+    Reyes::Projection projection(fovy, near_plane, ivec2(w, h));
+    mat2 sm;
+    projection.calc_screen_matrix(sm);
+    f2[0] = projection.f().x;
+    f2[1] = projection.f().y;
+    vp2[0] = sm[0][0];
+    vp2[1] = sm[1][1];
+}
+
 // The LIFO loop of src/Reyes/BoundNSplitCLCPU.cpp:75-159 and the range bound
 // of :249-336, written over the reference's eval_patch / eval_gregory_patch,
 // BBox, maximum and Projection::bound.

@@ -61,3 +61,38 @@ def test_reference_kernels_see_planted_oracle_change(built):
     q = oracle.make_params(sc, subpixel_bits=p.subpixel_bits - 1)
     col, dep, _ = oracle.render(sc, params=q)
     assert not np.array_equal(rd != EMPTY, dep != EMPTY)
+
+
+BOUND_CASES = [("heightfield_1024x768", {}), ("mixed96_bezier_512", {}), ("mixed96_gregory_512", {}),
+               ("mixed96_gregory_depth3_512", {}), ("heightfield_eye_plane_512x384", {}),
+               ("mixed96_bezier_512", {"bound_n_split_limit": 4.0, "cull_ribbon": 0.0}),
+               ("mixed96_gregory_512", {"bound_n_split_limit": 16.0, "cull_ribbon": 8.0})]
+
+
+@pytest.mark.parametrize("name,over", BOUND_CASES)
+def test_gpu_criterion_matches_reference_bound(built, name, over):
+    """The oracle's restatement of the reference's GPU bound criterion emits
+    the same sub-patch set, bit for bit, as bound() of
+    kernels/bound_n_split.h compiled as C++."""
+    from helpers import subpatch_set
+    oracle = _ref_lib()
+    if not hasattr(oracle.ref_pin(), "refk_bound_n_split_gpu"):
+        pytest.skip("reference tree not compiled here")
+    sc, _, _, _ = golden_case(name)
+    p = oracle.make_params(sc, bound_criterion=1, **over)
+    pid, rng, _ = oracle.bound_n_split(sc, params=p)
+    rpid, rrng = oracle.ref_bound_n_split_gpu(sc, params=p)
+    assert len(rpid) > 0
+    assert subpatch_set(pid, rng) == subpatch_set(rpid, rrng)
+
+
+def test_gpu_criterion_pin_sees_planted_change(built):
+    """A split limit 0.1 % lower in the oracle changes the set."""
+    from helpers import subpatch_set
+    oracle = _ref_lib()
+    sc, _, _, _ = golden_case("heightfield_1024x768")
+    p = oracle.make_params(sc, bound_criterion=1)
+    rpid, rrng = oracle.ref_bound_n_split_gpu(sc, params=p)
+    q = oracle.make_params(sc, bound_criterion=1, bound_n_split_limit=p.bound_n_split_limit * 0.999)
+    pid, rng, _ = oracle.bound_n_split(sc, params=q)
+    assert subpatch_set(pid, rng) != subpatch_set(rpid, rrng)
