@@ -285,6 +285,14 @@ __device__ __forceinline__ float ffma(float a, float b, float c) { return __fmaf
 __device__ __forceinline__ float frcp(float y) { return __frcp_rn(y); }
 __device__ __forceinline__ float kdiv(float x, float y) { return fmul(x, frcp(y)); }
 
+// Packed pairs (the FFMA2 / FMUL2 / FADD2 instructions of sm_100 and later):
+// each component rounds exactly as ffma / fmul / fadd, one instruction issue
+// for two.  The kernels pack the x/y and z/w components of one evaluation.
+__device__ __forceinline__ float2 ffma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 fmul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fadd2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 dup2(float a) { return make_float2(a, a); }
+
 // R6: sin/cos by Cody-Waite reduction with pi/2 = P1 + P2 + P3 (three floats
 // from the exact value of pi) and Taylor polynomials (degree 9 / 10) on
 // |r| <= pi/4, evaluated with fused multiply-adds.
@@ -339,24 +347,23 @@ __device__ __forceinline__ float4 col_weights(float ty) {
     return make_float4(fmul(fmul(sy, sy), sy), fmul(fmul(fmul(3.0f, ty), sy), sy), fmul(fmul(fmul(3.0f, ty), ty), sy),
                        fmul(fmul(ty, ty), ty));
 }
-// p += (v_i * c_j) * Q_{4i+j}, i-major, one fma per component (R1).
+// p += (v_i * c_j) * Q_{4i+j}, i-major, one fma per component (R1); the
+// x/y and z/w chains run as packed pairs.
 template <typename Pts>
 __device__ __forceinline__ float4 accumulate16(const Pts& Q, float4 vw4, float4 cw4) {
-    const float vw[4] = {vw4.x, vw4.y, vw4.z, vw4.w};
-    const float cw[4] = {cw4.x, cw4.y, cw4.z, cw4.w};
-    float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
+    const float2 vw[4] = {dup2(vw4.x), dup2(vw4.y), dup2(vw4.z), dup2(vw4.w)};
+    const float2 cw[4] = {dup2(cw4.x), dup2(cw4.y), dup2(cw4.z), dup2(cw4.w)};
+    float2 pxy = make_float2(0.f, 0.f), pzw = make_float2(0.f, 0.f);
 #pragma unroll
     for (int i = 0; i < 4; ++i)
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
-            float w = fmul(vw[i], cw[j]);
-            float4 c = Q[4 * i + j];
-            p.x = ffma(w, c.x, p.x);
-            p.y = ffma(w, c.y, p.y);
-            p.z = ffma(w, c.z, p.z);
-            p.w = ffma(w, c.w, p.w);
+            const float2 w = fmul2(vw[i], cw[j]);
+            const float4 c = Q[4 * i + j];
+            pxy = ffma2(w, make_float2(c.x, c.y), pxy);
+            pzw = ffma2(w, make_float2(c.z, c.w), pzw);
         }
-    return p;
+    return make_float4(pxy.x, pxy.y, pzw.x, pzw.y);
 }
 __device__ __forceinline__ float4 eval_bezier_dice_w(const float4* P, float4 vw, float4 cw) {
     return accumulate16(P, vw, cw);
@@ -366,9 +373,10 @@ __device__ __forceinline__ float4 eval_bezier_dice(const float4* P, float tx, fl
 }
 
 __device__ __forceinline__ float4 blend4(float a, float4 A, float b, float4 B, float den) {
-    const float r = frcp(den);
-    return make_float4(sel_nan(fmul(ffma(b, B.x, fmul(a, A.x)), r)), sel_nan(fmul(ffma(b, B.y, fmul(a, A.y)), r)),
-                       sel_nan(fmul(ffma(b, B.z, fmul(a, A.z)), r)), sel_nan(fmul(ffma(b, B.w, fmul(a, A.w)), r)));
+    const float2 r = dup2(frcp(den)), a2 = dup2(a), b2 = dup2(b);
+    const float2 xy = fmul2(ffma2(b2, make_float2(B.x, B.y), fmul2(a2, make_float2(A.x, A.y))), r);
+    const float2 zw = fmul2(ffma2(b2, make_float2(B.z, B.w), fmul2(a2, make_float2(A.z, A.w))), r);
+    return make_float4(sel_nan(xy.x), sel_nan(xy.y), sel_nan(zw.x), sel_nan(zw.y));
 }
 
 // kernels/utility.h:155-206 -- Gregory patch with NaN face blends zeroed.
@@ -385,13 +393,20 @@ __device__ __forceinline__ float4 eval_gregory_dice(const float4* P, float tx, f
     return eval_gregory_dice_w(P, tx, ty, row_weights(tx), col_weights(ty));
 }
 
-// dot products: a chain of fused multiply-adds from x to w (R1)
-__device__ __forceinline__ float dot4r(const float* m, int r, float4 v) {
-    return ffma(m[12 + r], v.w, ffma(m[8 + r], v.z, ffma(m[4 + r], v.y, fmul(m[r], v.x))));
-}
-// kernels/utility.h:174-180
+// kernels/utility.h:174-180: each row a dot product, a chain of fused
+// multiply-adds from x to w (R1); rows 0/1 and 2/3 as packed pairs (the
+// column-major m holds each pair of rows side by side).
 __device__ __forceinline__ float4 mul_m44v4(const float* m, float4 v) {
-    return make_float4(dot4r(m, 0, v), dot4r(m, 1, v), dot4r(m, 2, v), dot4r(m, 3, v));
+    const float2 x = dup2(v.x), y = dup2(v.y), z = dup2(v.z), w = dup2(v.w);
+    float2 r01 = fmul2(make_float2(m[0], m[1]), x);
+    float2 r23 = fmul2(make_float2(m[2], m[3]), x);
+    r01 = ffma2(make_float2(m[4], m[5]), y, r01);
+    r23 = ffma2(make_float2(m[6], m[7]), y, r23);
+    r01 = ffma2(make_float2(m[8], m[9]), z, r01);
+    r23 = ffma2(make_float2(m[10], m[11]), z, r23);
+    r01 = ffma2(make_float2(m[12], m[13]), w, r01);
+    r23 = ffma2(make_float2(m[14], m[15]), w, r23);
+    return make_float4(r01.x, r01.y, r23.x, r23.y);
 }
 
 // kernels/dice.cl:51-67 -- eye-space displacement, updated coordinates used
@@ -439,10 +454,13 @@ __device__ __forceinline__ void project_vertex_m(const float* proj, const FrameD
     float4 p = mul_m44v4(proj, pos);
     int vsx = fr.W << fr.shift, vsy = fr.H << fr.shift;
     const float rw = frcp(p.w);
-    float ex = fadd(fmul(fmul(fmul(p.x, rw), (float)vsx), 0.5f), (float)(vsx / 2));
-    float ey = fadd(fmul(fmul(fmul(p.y, rw), (float)vsy), 0.5f), (float)(vsy / 2));
-    px = __float2int_rz(ex);
-    py = __float2int_rz(ey);
+    // (p.xy / p.w * VIEWPORT_SIZE) / 2 + VIEWPORT_SIZE / 2, x and y packed
+    float2 e = fmul2(make_float2(p.x, p.y), dup2(rw));
+    e = fmul2(e, make_float2((float)vsx, (float)vsy));
+    e = fmul2(e, dup2(0.5f));
+    e = fadd2(e, make_float2((float)(vsx / 2), (float)(vsy / 2)));
+    px = __float2int_rz(e.x);
+    py = __float2int_rz(e.y);
     depth = fmul(p.z, rw);
 }
 __device__ __forceinline__ void project_vertex(const DrawDev& d, const FrameDev& fr, float4 pos, int& px, int& py,
