@@ -11,7 +11,10 @@
 //   * dice / shade / sample (kernels/dice.cl, kernels/reyes.cl,
 //     kernels/utility.h): the rounding choices allowed by the reference's
 //     -cl-mad-enable -cl-fast-relaxed-math build are fixed as
-//       R1 a*b + c is one fma; a*b + c*d = fma(c, d, a*b); a*b - c*d = fma(-c, d, a*b)
+//       R1 a*b + c is one fma; dot() fuses its first product,
+//          fma(w, w', fma(z, z', fma(x, x', y*y'))); the barycentric dot and
+//          vector sums a*A + b*B (Gregory blends, colour) fuse the later one,
+//          fma(b, B, a*A); cross(): a*b - c*d = fma(-c, d, a*b)
 //       R2 a division x / y is x * RN(1 / y) (the reciprocal correctly rounded,
 //          as -cl-fast-relaxed-math permits); sqrt correctly rounded
 //       R3 max(x, 0) ignores NaN (fmaxf)
@@ -79,6 +82,15 @@ __device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b)
 __device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
 __device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
 __device__ __forceinline__ float fdiv(float a, float b) { return __fdiv_rn(a, b); }
+
+// Packed pairs (the FFMA2 / FMUL2 / FADD2 instructions of sm_100 and later):
+// each component rounds exactly as ffma / fmul / fadd, one instruction issue
+// for two.  The kernels pack the x/y (and z/w) components of one evaluation.
+__device__ __forceinline__ float2 ffma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 fmul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fadd2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 dup2(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 xy2(const F3& p) { return make_float2(p.x, p.y); }
 // src/base/utility.h:86-94
 __device__ __forceinline__ float minimum(float a, float b) { return a < b ? a : b; }
 __device__ __forceinline__ float maximum(float a, float b) { return a > b ? a : b; }
@@ -108,18 +120,19 @@ __device__ __forceinline__ F3 ld3(const float4* p) {
 }
 
 // glm 0.9.9 mat4 * vec4(p, 1): (m0*x + m1*y) + (m2*z + m3*1), per component.
+// Rows x and y as one packed pair, z alone.
 __device__ __forceinline__ F3 mv_point(const float* m, const F3& p) {
-    F3 r;
-    r.x = fadd(fadd(fmul(m[0], p.x), fmul(m[4], p.y)), fadd(fmul(m[8], p.z), fmul(m[12], 1.0f)));
-    r.y = fadd(fadd(fmul(m[1], p.x), fmul(m[5], p.y)), fadd(fmul(m[9], p.z), fmul(m[13], 1.0f)));
-    r.z = fadd(fadd(fmul(m[2], p.x), fmul(m[6], p.y)), fadd(fmul(m[10], p.z), fmul(m[14], 1.0f)));
-    return r;
+    const float2 xy = fadd2(fadd2(fmul2(make_float2(m[0], m[1]), dup2(p.x)), fmul2(make_float2(m[4], m[5]), dup2(p.y))),
+                            fadd2(fmul2(make_float2(m[8], m[9]), dup2(p.z)), fmul2(make_float2(m[12], m[13]), dup2(1.0f))));
+    return F3{xy.x, xy.y, fadd(fadd(fmul(m[2], p.x), fmul(m[6], p.y)), fadd(fmul(m[10], p.z), fmul(m[14], 1.0f)))};
 }
 
 // glm::distance: sqrt((dx*dx + dy*dy) + dz*dz)
 __device__ __forceinline__ float distance3(const F3& a, const F3& b) {
-    float dx = fsub(b.x, a.x), dy = fsub(b.y, a.y), dz = fsub(b.z, a.z);
-    return __fsqrt_rn(fadd(fadd(fmul(dx, dx), fmul(dy, dy)), fmul(dz, dz)));
+    const float2 d = fadd2(xy2(b), make_float2(-a.x, -a.y));   // b - a, exactly as fsub
+    const float2 d2 = fmul2(d, d);
+    const float dz = fsub(b.z, a.z);
+    return __fsqrt_rn(fadd(fadd(d2.x, d2.y), fmul(dz, dz)));
 }
 
 // Gregory patch (src/base/Patch.cpp:186-210), evaluated at (u, v) after the swap.
@@ -285,13 +298,6 @@ __device__ __forceinline__ float ffma(float a, float b, float c) { return __fmaf
 __device__ __forceinline__ float frcp(float y) { return __frcp_rn(y); }
 __device__ __forceinline__ float kdiv(float x, float y) { return fmul(x, frcp(y)); }
 
-// Packed pairs (the FFMA2 / FMUL2 / FADD2 instructions of sm_100 and later):
-// each component rounds exactly as ffma / fmul / fadd, one instruction issue
-// for two.  The kernels pack the x/y and z/w components of one evaluation.
-__device__ __forceinline__ float2 ffma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
-__device__ __forceinline__ float2 fmul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
-__device__ __forceinline__ float2 fadd2(float2 a, float2 b) { return __fadd2_rn(a, b); }
-__device__ __forceinline__ float2 dup2(float a) { return make_float2(a, a); }
 
 // R6: sin/cos by Cody-Waite reduction with pi/2 = P1 + P2 + P3 (three floats
 // from the exact value of pi) and Taylor polynomials (degree 9 / 10) on
@@ -393,15 +399,15 @@ __device__ __forceinline__ float4 eval_gregory_dice(const float4* P, float tx, f
     return eval_gregory_dice_w(P, tx, ty, row_weights(tx), col_weights(ty));
 }
 
-// kernels/utility.h:174-180: each row a dot product, a chain of fused
-// multiply-adds from x to w (R1); rows 0/1 and 2/3 as packed pairs (the
+// kernels/utility.h:174-180: each row a dot(), fma(w, w', fma(z, z',
+// fma(x, x', y*y'))) (R1); rows 0/1 and 2/3 as packed pairs (the
 // column-major m holds each pair of rows side by side).
 __device__ __forceinline__ float4 mul_m44v4(const float* m, float4 v) {
     const float2 x = dup2(v.x), y = dup2(v.y), z = dup2(v.z), w = dup2(v.w);
-    float2 r01 = fmul2(make_float2(m[0], m[1]), x);
-    float2 r23 = fmul2(make_float2(m[2], m[3]), x);
-    r01 = ffma2(make_float2(m[4], m[5]), y, r01);
-    r23 = ffma2(make_float2(m[6], m[7]), y, r23);
+    float2 r01 = fmul2(make_float2(m[4], m[5]), y);
+    float2 r23 = fmul2(make_float2(m[6], m[7]), y);
+    r01 = ffma2(make_float2(m[0], m[1]), x, r01);
+    r23 = ffma2(make_float2(m[2], m[3]), x, r23);
     r01 = ffma2(make_float2(m[8], m[9]), z, r01);
     r23 = ffma2(make_float2(m[10], m[11]), z, r23);
     r01 = ffma2(make_float2(m[12], m[13]), w, r01);
@@ -469,7 +475,8 @@ __device__ __forceinline__ void project_vertex(const DrawDev& d, const FrameDev&
 }
 
 struct V3 { float x, y, z; };
-__device__ __forceinline__ float dot3(V3 a, V3 b) { return ffma(a.z, b.z, ffma(a.y, b.y, fmul(a.x, b.x))); }
+// dot(): fma(z, z', fma(x, x', y*y')) (R1)
+__device__ __forceinline__ float dot3(V3 a, V3 b) { return ffma(a.z, b.z, ffma(a.x, b.x, fmul(a.y, b.y))); }
 __device__ __forceinline__ V3 cross3(V3 a, V3 b) {
     return V3{ffma(-a.z, b.y, fmul(a.y, b.z)), ffma(-a.x, b.z, fmul(a.z, b.x)), ffma(-a.y, b.x, fmul(a.x, b.y))};
 }
@@ -619,14 +626,14 @@ __device__ __forceinline__ int bns_decide_gpu(const DrawDev& d, const FrameDev& 
             const float x = fmul(q.x, rw), y = fmul(q.y, rw);
             // mul_cm2v2(screen_matrix = diag(vp), (x, y)): m0 * x + m1 * y per component
             const float2 s = make_float2(ffma(0.0f, y, fmul(d.vpx, x)), ffma(d.vpy, y, fmul(0.0f, x)));
-            // distance(a, b) = sqrt(dx*dx + dy*dy), R1: fma(dy, dy, dx*dx)
+            // distance(a, b) = sqrt(dot(a - b, a - b)), R1: fma(dx, dx, dy*dy)
             if (v > 0) {
                 const float dx = fsub(above.x, s.x), dy = fsub(above.y, s.y);
-                vsum = fadd(vsum, __fsqrt_rn(ffma(dy, dy, fmul(dx, dx))));
+                vsum = fadd(vsum, __fsqrt_rn(ffma(dx, dx, fmul(dy, dy))));
             }
             if (u > 0) {
                 const float dx = fsub(prev[v].x, s.x), dy = fsub(prev[v].y, s.y);
-                hsum[v] = fadd(hsum[v], __fsqrt_rn(ffma(dy, dy, fmul(dx, dx))));
+                hsum[v] = fadd(hsum[v], __fsqrt_rn(ffma(dx, dx, fmul(dy, dy))));
             }
             above = s;
             prev[v] = s;

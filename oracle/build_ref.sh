@@ -29,8 +29,11 @@ done
 # The reference's kernels (kernels/*.cl) rewritten into C++ by clshim/rewrite.py,
 # into _ref/kernels/ only, then compiled with the fiber runtime ref_kernels.cpp.
 python3 "$HERE/clshim/rewrite.py" "$REF/kernels" "$OUT/kernels"
+# the oracle's sine stands for native_sin (clshim/cl_shim.h)
+g++ $COMMON -ffp-contract=off -fopenmp -c "$HERE/oracle.cpp" -o "$OUT/obj/oracle.o" &
+PIDS="$PIDS $!"
 g++ $COMMON $FMA -ffp-contract=fast -I "$HERE" -c "$HERE/ref_kernels.cpp" -o "$OUT/obj/ref_kernels.o"
 for p in $PIDS; do wait "$p"; done
-g++ -shared -pthread "$OUT/obj/Patch.o" "$OUT/obj/Projection.o" "$OUT/obj/ref_pin.o" "$OUT/obj/ref_kernels.o" \
-    -o "$OUT/libref_pin.so"
+g++ -shared -pthread -fopenmp "$OUT/obj/Patch.o" "$OUT/obj/Projection.o" "$OUT/obj/ref_pin.o" \
+    "$OUT/obj/ref_kernels.o" "$OUT/obj/oracle.o" -o "$OUT/libref_pin.so"
 echo "build_ref: $OUT/libref_pin.so"

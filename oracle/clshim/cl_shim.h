@@ -3,10 +3,16 @@
 // INFRASTRUCTURE ONLY.  Vectors are unions of their components and read-only
 // swizzle views (v.xyz converts to a float3), component-wise operators,
 // comparisons giving -1 / 0 masks, and the work-item functions of the
-// fiber runtime in ref_kernels.cpp.  Arithmetic is IEEE float with the
-// floating-point contraction of the build (the reference builds with
-// -cl-fast-relaxed-math -cl-mad-enable, which leaves rounding open;
-// comparisons against the oracle allow for it).
+// fiber runtime in ref_kernels.cpp.
+//
+// The reference builds its kernels with -cl-fast-relaxed-math
+// -cl-mad-enable, which leave the rounding of contractions, divisions,
+// float-to-int conversions and native_sin open.  The shim fixes them as the
+// oracle does: contraction is the compiler's (a*b + c*d fuses the first
+// product, as gcc and LLVM contract), a float division x / y is
+// x * RN(1 / y) (the vector operators here; rewrite.py routes the scalar ones
+// through cl_fdiv), (int) of a float truncates and saturates with NaN -> 0
+// (cl_f2i), and native_sin is the oracle's sine (or_sinf).
 #pragma once
 #include <cmath>
 #include <cstddef>
@@ -14,14 +20,14 @@
 
 namespace clshim {
 
-template <class E, class R, int... I>
+// x / y: x * RN(1 / y) for floats, integer division for ints
+inline float div(float x, float y) { return x * (1.0f / y); }
+inline int div(int x, int y) { return x / y; }
+
+// N: the components of the vector the view lies in (its size must not grow).
+template <class E, class R, int N, int... I>
 struct Swz {
-    E s[4];
-    operator R() const { return R(s[I]...); }
-};
-template <class E, class R, int... I>
-struct Swz16 {
-    E s[16];
+    E s[N];
     operator R() const { return R(s[I]...); }
 };
 
@@ -31,7 +37,7 @@ struct Swz16 {
     inline T operator+(T a, T b) { T r; for (int i = 0; i < N; ++i) r.s[i] = a.s[i] + b.s[i]; return r; } \
     inline T operator-(T a, T b) { T r; for (int i = 0; i < N; ++i) r.s[i] = a.s[i] - b.s[i]; return r; } \
     inline T operator*(T a, T b) { T r; for (int i = 0; i < N; ++i) r.s[i] = a.s[i] * b.s[i]; return r; } \
-    inline T operator/(T a, T b) { T r; for (int i = 0; i < N; ++i) r.s[i] = a.s[i] / b.s[i]; return r; } \
+    inline T operator/(T a, T b) { T r; for (int i = 0; i < N; ++i) r.s[i] = clshim::div(a.s[i], b.s[i]); return r; } \
     inline T operator+(T a, E b) { return a + T(b); }                                           \
     inline T operator-(T a, E b) { return a - T(b); }                                           \
     inline T operator*(T a, E b) { return a * T(b); }                                           \
@@ -67,8 +73,8 @@ struct int2 {
     union {
         int s[2];
         struct { int x, y; };
-        clshim::Swz<int, int3, 0, 0, 0> xxx;
-        clshim::Swz<int, int3, 1, 1, 1> yyy;
+        clshim::Swz<int, int3, 2, 0, 0, 0> xxx;
+        clshim::Swz<int, int3, 2, 1, 1, 1> yyy;
     };
     int2() : s{0, 0} {}
     int2(int a) : s{a, a} {}
@@ -78,7 +84,7 @@ struct float3 {
     union {
         float s[4];
         struct { float x, y, z; };
-        clshim::Swz<float, float3, 1, 2, 0> yzx;
+        clshim::Swz<float, float3, 4, 1, 2, 0> yzx;
     };
     float3() : s{0, 0, 0, 0} {}
     explicit float3(float a) : s{a, a, a, 0} {}
@@ -88,7 +94,7 @@ struct int3 {
     union {
         int s[4];
         struct { int x, y, z; };
-        clshim::Swz<int, int3, 1, 2, 0> yzx;
+        clshim::Swz<int, int3, 4, 1, 2, 0> yzx;
     };
     int3() : s{0, 0, 0, 0} {}
     int3(int a) : s{a, a, a, 0} {}
@@ -98,10 +104,10 @@ struct float4 {
     union {
         float s[4];
         struct { float x, y, z, w; };
-        clshim::Swz<float, float3, 0, 1, 2> xyz;
-        clshim::Swz<float, float3, 0, 1, 3> xyw;
-        clshim::Swz<float, float3, 0, 3, 2> xwz;
-        clshim::Swz<float, float2, 0, 1> xy;
+        clshim::Swz<float, float3, 4, 0, 1, 2> xyz;
+        clshim::Swz<float, float3, 4, 0, 1, 3> xyw;
+        clshim::Swz<float, float3, 4, 0, 3, 2> xwz;
+        clshim::Swz<float, float2, 4, 0, 1> xy;
     };
     float4() : s{0, 0, 0, 0} {}
     explicit float4(float a) : s{a, a, a, a} {}
@@ -111,11 +117,11 @@ struct int4 {
     union {
         int s[4];
         struct { int x, y, z, w; };
-        clshim::Swz<int, int3, 0, 1, 3> xyw;
-        clshim::Swz<int, int3, 0, 3, 2> xwz;
-        clshim::Swz<int, int2, 0, 1> xy;
-        clshim::Swz<int, int2, 2, 3> zw;
-        clshim::Swz<int, int2, 2, 0> zx;
+        clshim::Swz<int, int3, 4, 0, 1, 3> xyw;
+        clshim::Swz<int, int3, 4, 0, 3, 2> xwz;
+        clshim::Swz<int, int2, 4, 0, 1> xy;
+        clshim::Swz<int, int2, 4, 2, 3> zw;
+        clshim::Swz<int, int2, 4, 2, 0> zx;
     };
     int4() : s{0, 0, 0, 0} {}
     int4(int a) : s{a, a, a, a} {}
@@ -124,13 +130,17 @@ struct int4 {
 struct float16 {
     union {
         float s[16];
-        clshim::Swz16<float, float4, 0, 4, 8, 12> s048C;
-        clshim::Swz16<float, float4, 1, 5, 9, 13> s159D;
-        clshim::Swz16<float, float4, 2, 6, 10, 14> s26AE;
-        clshim::Swz16<float, float4, 3, 7, 11, 15> s37BF;
+        clshim::Swz<float, float4, 16, 0, 4, 8, 12> s048C;
+        clshim::Swz<float, float4, 16, 1, 5, 9, 13> s159D;
+        clshim::Swz<float, float4, 16, 2, 6, 10, 14> s26AE;
+        clshim::Swz<float, float4, 16, 3, 7, 11, 15> s37BF;
     };
     float16() : s{} {}
 };
+
+static_assert(sizeof(float2) == 8 && sizeof(int2) == 8 && sizeof(float3) == 16 && sizeof(int3) == 16 &&
+                  sizeof(float4) == 16 && sizeof(int4) == 16 && sizeof(float16) == 64,
+              "OpenCL vector sizes");
 
 CLSHIM_VEC_OPS(float2, float, 2)
 CLSHIM_VEC_OPS(float3, float, 3)
@@ -181,7 +191,15 @@ inline int2 max(int2 a, int2 b) { return int2(max(a.x, b.x), max(a.y, b.y)); }
 inline int2 min(int2 a, int2 b) { return int2(min(a.x, b.x), min(a.y, b.y)); }
 inline float clamp(float x, float a, float b) { return std::fmin(std::fmax(x, a), b); }
 inline int2 clamp(int2 v, int a, int b) { return int2(min(max(v.x, a), b), min(max(v.y, a), b)); }
-inline float native_sin(float x) { return std::sin(x); }
+extern "C" float or_sinf(float x);
+inline float native_sin(float x) { return or_sinf(x); }
+inline float cl_fdiv(float x, float y) { return clshim::div(x, y); }
+inline int cl_f2i(float x) {
+    if (std::isnan(x)) return 0;
+    if (x >= 2147483648.0f) return 2147483647;
+    if (x <= -2147483648.0f) return (-2147483647 - 1);
+    return (int)x;
+}
 inline int4 isnan(float4 v) {
     return int4(std::isnan(v.x) ? -1 : 0, std::isnan(v.y) ? -1 : 0, std::isnan(v.z) ? -1 : 0, std::isnan(v.w) ? -1 : 0);
 }

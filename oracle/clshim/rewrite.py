@@ -8,7 +8,10 @@ Only what C++ cannot express through the shim is rewritten:
     `static thread_local` (one work-group runs on one host thread at a time);
   * `volatile global` buffers lose the volatile (their atomics go through the
     shim, plain stores need no volatile);
-  * OpenCL's component-wise ?: on an int3 condition becomes vselect3().
+  * OpenCL's component-wise ?: on an int3 condition becomes vselect3();
+  * the scalar float divisions (p.x/p.w, depth / 200.0f and the four of
+    outside_frustum) become cl_fdiv() and the (int) casts of floats cl_f2i(),
+    the shim's fixed choices for what -cl-fast-relaxed-math leaves open.
 Everything else (swizzles, built-ins, operators) is the shim's.
 
     python oracle/clshim/rewrite.py <reference kernels dir> <output dir>
@@ -27,6 +30,10 @@ def rewrite(text: str) -> str:
     text = re.sub(r"volatile\s+(__)?global\b", "global", text)
     text = re.sub(r"(\([^;?]*\))\s*\?\s*int3\(\s*-1\s*,\s*-1\s*,\s*-1\s*\)\s*:\s*int3\(\s*0\s*,\s*0\s*,\s*0\s*\)",
                   r"vselect3(\1, int3(-1, -1, -1), int3(0, 0, 0))", text)
+    text = re.sub(r"\b(p\.[xyz])/p\.w\b", r"cl_fdiv(\1, p.w)", text)
+    text = re.sub(r"\bdepth / 200\.0f", "cl_fdiv(depth, 200.0f)", text)
+    text = re.sub(r"\b(p(?:min|max)\.[xy])/(\(\(p(?:min|max)\.[xy] [<>] 0\) \? n : f\))", r"cl_fdiv(\1, \2)", text)
+    text = re.sub(r"\(int\)\(", "cl_f2i(", text)
     return text
 
 

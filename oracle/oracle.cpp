@@ -8,10 +8,17 @@
 // Arithmetic conventions of the kernel restatement.  The reference kernels
 // are built with -cl-fast-relaxed-math -cl-mad-enable (src/CL/Program.cpp:118),
 // which leaves rounding open.  This restatement fixes one admissible choice
-// and the CUDA kernels follow the same one:
+// and the CUDA kernels follow the same one.  Where a sum of products leaves a
+// choice, R1 takes the one gcc 13 makes when it compiles the kernel source
+// itself with contraction on (oracle/ref_kernels.cpp, the pin in
+// tests/test_refkernels_cpu.py, which reproduces this oracle's frames):
 //   R1  an expression a*b + c (or c + a*b) is one fused multiply-add;
-//       a*b + c*d is fma(c, d, a*b) (right product fused);
-//       a*b - c*d is fma(-c, d, a*b);
+//       dot() (mul_m44v4's rows, shading, distance) fuses the first product:
+//       dot(a, b) = fma(a.w, b.w, fma(a.z, b.z, fma(a.x, b.x, a.y*b.y)));
+//       the barycentric dot of inside_triangle and the vector sums
+//       a*A + b*B (Gregory blends, mul_cm2v2, mul_pm4v4 / mul_cm4v4, the
+//       colour ac*dc + m*dc) fuse the later product: fma(b, B, a*A);
+//       cross() components a*b - c*d are fma(-c, d, a*b);
 //   R2  a division x / y is x * RN(1 / y), the reciprocal correctly rounded
 //       (-cl-fast-relaxed-math permits it); square root is correctly rounded;
 //   R3  max(x, 0) on floats ignores a NaN operand (fmaxf);
@@ -407,12 +414,13 @@ static inline V4 eval_gregory_k(const float* cp, float tx, float ty) {
     return p;
 }
 
-// dot products (R1: a chain of fused multiply-adds from x to w)
+// dot() (R1: x*x' + y*y' is fma(x, x', y*y'), then one fused multiply-add
+// per further term)
 static inline float dot4(const float* a, const V4& b) {
-    return std::fma(a[3], b.w, std::fma(a[2], b.z, std::fma(a[1], b.y, a[0] * b.x)));
+    return std::fma(a[3], b.w, std::fma(a[2], b.z, std::fma(a[0], b.x, a[1] * b.y)));
 }
 static inline float dot3(const V3& a, const V3& b) {
-    return std::fma(a.z, b.z, std::fma(a.y, b.y, a.x * b.x));
+    return std::fma(a.z, b.z, std::fma(a.x, b.x, a.y * b.y));
 }
 
 // kernels/utility.h:174-180 -- row r of a column-major float16 is (m[r], m[4+r], m[8+r], m[12+r]).
@@ -502,8 +510,8 @@ static int bound_gpu(const or_params* P, const or_draw* d, const PatchRange& r) 
         for (int j = 0; j < 2; ++j) {
             float hx = pp[i][j].x - pp[i][j + 1].x, hy = pp[i][j].y - pp[i][j + 1].y;
             float vx = pp[j][i].x - pp[j + 1][i].x, vy = pp[j][i].y - pp[j + 1][i].y;
-            h += std::sqrt(std::fma(hy, hy, hx * hx));
-            v += std::sqrt(std::fma(vy, vy, vx * vx));
+            h += std::sqrt(std::fma(hx, hx, hy * hy));
+            v += std::sqrt(std::fma(vx, vx, vy * vy));
         }
         hlen = std::fmax(h, hlen);
         vlen = std::fmax(v, vlen);
@@ -925,6 +933,30 @@ extern "C" void or_dice(const or_params* p, const or_draw* d, int32_t pid, const
             pos[4 * i + 1] = ps.y;
             pos[4 * i + 2] = ps.z;
             pos[4 * i + 3] = ps.w;
+        }
+}
+
+// kernels/reyes.cl:172-191 for every quad of one sub-patch: colour q =
+// nu + nv * PS (the colour grid of calc_color_grid_pos), whether or not its
+// 8x8 block is empty.
+extern "C" void or_shade_quads(const or_params* p, const or_draw* d, int32_t pid, const float range[4],
+                               float* color) {
+    const int PS = p->reyes_patch_size, G = PS + 1;
+    std::vector<float> pos((size_t)G * G * 4), dep((size_t)G * G);
+    std::vector<int32_t> pxl((size_t)G * G * 2);
+    or_dice(p, d, pid, range, pos.data(), pxl.data(), dep.data());
+    Frame f;
+    f.P = p;
+    for (int nv = 0; nv < PS; ++nv)
+        for (int nu = 0; nu < PS; ++nu) {
+            V4 q[4];
+            for (int k = 0; k < 4; ++k) {
+                const int gi = (nu + (k & 1)) + (nv + (k >> 1)) * G;
+                q[k] = V4{pos[4 * gi], pos[4 * gi + 1], pos[4 * gi + 2], pos[4 * gi + 3]};
+            }
+            const V4 c = f.shade(q, d->color);
+            float* o = color + 4 * (nu + nv * PS);
+            o[0] = c.x; o[1] = c.y; o[2] = c.z; o[3] = c.w;
         }
 }
 

@@ -86,6 +86,7 @@ void or_dice(const or_params* p, const or_draw* d, int32_t pid, const float rang
              float* pos, int32_t* pxl, float* depth);
 
 /* FP64 Bernstein dice of the same vertices (eye space, after displacement). */
+void or_shade_quads(const or_params* p, const or_draw* d, int32_t pid, const float range[4], float* color);
 void or_dice_fp64(const or_params* p, const or_draw* d, int32_t pid, const float range[4],
                   double* pos3);
 

@@ -66,6 +66,8 @@ def lib():
         L.or_dice.restype = None
         L.or_dice.argtypes = [ctypes.POINTER(OrParams), ctypes.POINTER(OrDraw), ctypes.c_int32, f32p, f32p,
                               i32p, f32p]
+        L.or_shade_quads.restype = None
+        L.or_shade_quads.argtypes = [ctypes.POINTER(OrParams), ctypes.POINTER(OrDraw), ctypes.c_int32, f32p, f32p]
         L.or_dice_fp64.restype = None
         L.or_dice_fp64.argtypes = [ctypes.POINTER(OrParams), ctypes.POINTER(OrDraw), ctypes.c_int32, f32p,
                                    f64p]
@@ -186,6 +188,17 @@ def dice(scene, draw_index, pid, rng, params=None):
     return pos, pxl, dep
 
 
+def shade_quads(scene, draw_index, pid, rng, params=None):
+    """Colour of every quad of one sub-patch (kernels/reyes.cl:172-191),
+    float32[PS*PS, 4] in colour-grid order nu + nv * PS."""
+    p = params or make_params(scene)
+    ds = _Draws([scene.draws[draw_index]])
+    col = np.zeros((p.reyes_patch_size ** 2, 4), np.float32)
+    r = np.ascontiguousarray(rng, np.float32)
+    lib().or_shade_quads(ctypes.byref(p), ds.arr, int(pid), _ptr(r, f32p), _ptr(col, f32p))
+    return col
+
+
 def dice_fp64(scene, draw_index, pid, rng, params=None):
     p = params or make_params(scene)
     ds = _Draws([scene.draws[draw_index]])
@@ -264,6 +277,42 @@ def ref_bound_n_split(scene, draw_index=0, params=None):
     rng = np.zeros((max(n, 1), 4), np.float32)
     L.refpin_bound_n_split(*args, _ptr(pid, i32p), _ptr(rng, f32p), n)
     return pid[:n], rng[:n]
+
+
+def ref_dice_shade(scene, draw_index, pid, rng, params=None, threads=None):
+    """The reference's dice and shade kernels (compiled as C++ by
+    oracle/build_ref.sh) over sub-patches (pid[S], range[S,4]) of one draw:
+    (pos float32[S,G*G,4], pxl int32[S,G*G,2], depth float32[S,G*G],
+    colour float32[S,PS*PS,4] with NaN where shade left a quad unwritten,
+    block bounds int32[S,B,4]), or None where the reference tree was not
+    compiled."""
+    L = ref_pin()
+    if L is None or not hasattr(L, "refk_dice_shade"):
+        return None
+    p = params or make_params(scene)
+    d = scene.draws[draw_index]
+    PS = p.reyes_patch_size
+    G, B, S = PS + 1, (PS // 8) ** 2, len(pid)
+    cp = np.ascontiguousarray(d.mesh.cp, np.float32).reshape(-1)
+    mv = np.ascontiguousarray(d.mv, np.float32)
+    dc = np.asarray(d.color, np.float32)
+    pids = np.ascontiguousarray(pid, np.int32)
+    rg = np.ascontiguousarray(rng, np.float32)
+    pos = np.zeros((S, G * G, 4), np.float32)
+    pxl = np.zeros((S, G * G, 2), np.int32)
+    dep = np.zeros((S, G * G), np.float32)
+    col = np.full((S, PS * PS, 4), np.nan, np.float32)
+    blk = np.zeros((S, B, 4), np.int32)
+    f = L.refk_dice_shade
+    f.restype = None
+    f.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_float, ctypes.c_float, ctypes.c_int, ctypes.c_int,
+                  ctypes.c_int, ctypes.c_int, f32p, ctypes.c_int, ctypes.c_int, f32p, f32p, ctypes.c_int, i32p,
+                  f32p, f32p, i32p, f32p, f32p, i32p, ctypes.c_int]
+    f(p.width, p.height, p.fovy_deg, p.near_plane, PS, p.subpixel_bits, p.backface_culling, p.displacement,
+      _ptr(cp, f32p), d.mesh.n_patches, d.mesh.type, _ptr(mv, f32p), _ptr(dc, f32p), S, _ptr(pids, i32p),
+      _ptr(rg, f32p), _ptr(pos, f32p), _ptr(pxl, i32p), _ptr(dep, f32p), _ptr(col, f32p), _ptr(blk, i32p),
+      int(threads or os.cpu_count() or 1))
+    return pos, pxl, dep, col, blk
 
 
 def ref_bound_n_split_gpu(scene, draw_index=0, params=None):

@@ -242,6 +242,64 @@ long refk_bound_n_split_gpu(const float* cp_in, int n_patches, int type, const f
     return n;
 }
 
+// The reference's dice and shade kernels over `count` sub-patches of one
+// draw in one pass (RendererCL.cpp:203-238): the position, pixel and depth
+// grids ((PS+1)^2 per sub-patch), the colour grid (PS^2 per sub-patch, left
+// untouched where shade returns early for an empty block) and the block
+// bounds (int4 per 8x8 block).
+void refk_dice_shade(int W, int H, float fovy, float near_plane, int patch_size, int subpixel_bits, int backface,
+                     int displacement, const float* cp_in, int n_patches, int type, const float* mv16,
+                     const float* color, int count, const int* pids, const float* ranges, float* pos_out,
+                     int* pxl_out, float* dep_out, float* col_out, int* block_out, int threads) {
+    g_cfg.patch_size = patch_size;
+    g_cfg.pxl_shift = subpixel_bits;
+    g_cfg.backface = backface;
+    g_cfg.displacement = displacement;
+    g_cfg.fb_size = int2(W, H);
+    g_cfg.grid_size = int2((W + 7) / 8, (H + 7) / 8);
+    g_cfg.vp_min_px = int2(0, 0);
+    g_cfg.vp_max_px = int2(W, H);
+    g_cfg.vp_size_px = int2(W, H);
+    const int per = type == 0 ? 16 : 20;
+    std::vector<float4> patch((size_t)n_patches * per);
+    for (size_t k = 0; k < patch.size(); ++k)
+        patch[k] = float4(cp_in[3 * k], cp_in[3 * k + 1], cp_in[3 * k + 2], 1.0f);
+    float proj16[16];
+    refpin_projection_matrix(fovy, near_plane, W, H, proj16);
+    float16 proj, mv;
+    for (int k = 0; k < 16; ++k) {
+        proj.s[k] = proj16[k];
+        mv.s[k] = mv16[k];
+    }
+    std::vector<float2> mins((size_t)count), maxs((size_t)count);
+    for (int s = 0; s < count; ++s) {
+        mins[(size_t)s] = float2(ranges[4 * s], ranges[4 * s + 1]);
+        maxs[(size_t)s] = float2(ranges[4 * s + 2], ranges[4 * s + 3]);
+    }
+    float4* pos = reinterpret_cast<float4*>(pos_out);
+    int2* pxl = reinterpret_cast<int2*>(pxl_out);
+    float4* col = reinterpret_cast<float4*>(col_out);
+    int4* blocks = reinterpret_cast<int4*>(block_out);
+    const float4 dc(color[0], color[1], color[2], color[3]);
+    const int gw = 8;
+    {
+        const size_t glb[3] = {(size_t)(patch_size + gw), (size_t)(patch_size + gw), (size_t)count};
+        const size_t loc[3] = {(size_t)gw, (size_t)gw, 1};
+        std::function<void()> body = [&]() {
+            if (type == 0)
+                refk_bezier::dice(patch.data(), pids, mins.data(), maxs.data(), pos, pxl, dep_out, mv, proj);
+            else
+                refk_gregory::dice(patch.data(), pids, mins.data(), maxs.data(), pos, pxl, dep_out, mv, proj);
+        };
+        launch(body, glb, loc, threads);
+    }
+    {
+        const size_t glb[3] = {(size_t)patch_size, (size_t)patch_size, (size_t)count}, loc[3] = {8, 8, 1};
+        std::function<void()> body = [&]() { refk_reyes::shade(pos, pxl, blocks, col, dc); };
+        launch(body, glb, loc, threads);
+    }
+}
+
 // One frame as RendererCL draws it: clear (kernels/framebuffer.cl and the
 // depth fill of RendererCL.cpp:115-135), then per draw the reference's CPU
 // bound-and-split and, per pass of at most patches_per_pass sub-patches,

@@ -3,13 +3,14 @@ kernels (kernels/dice.cl, kernels/reyes.cl, kernels/framebuffer.cl), compiled
 as C++ by oracle/build_ref.sh and run on the CPU with the launch geometry of
 src/Reyes/RendererCL.cpp after the reference's CPU bound-and-split.
 
-Both sides compute in FP32 with fused multiply-adds, but gcc contracts the
-kernel source where it chooses and divides with IEEE `/`, while the oracle
-fixes one contraction per expression and divides by a reciprocal (the
-arithmetic the CUDA kernels use).  So the frames agree to rounding, not bit
-for bit: pixel coverage exactly, depth keys within a few units of the 2^31
-scale, colours within 1e-3 relative in all but a few pixels (quads whose
-normal comes from nearly equal positions amplify the rounding).
+The reference's -cl-fast-relaxed-math build leaves the rounding of
+contractions, divisions, float-to-int conversions and native_sin open; the
+compiled kernels take the oracle's choices for the last three (the shim) and
+gcc's own contraction, which the oracle's R1 table follows.  So the diced
+grids agree bit for bit, and the frames meet the bar of the benchmark spec:
+depth and colour within 1e-5 relative per pixel except in fewer than 1e-4
+of the frame's pixels (tie pixels, where the two sides let a different one
+of two equally deep micropolygons win).
 """
 import numpy as np
 import pytest
@@ -41,14 +42,36 @@ def test_oracle_frame_matches_reference_kernels(built, name, disp):
     cov_r, cov_o = rd != EMPTY, dep != EMPTY
     assert cov_r.sum() > 0
     assert np.array_equal(cov_r, cov_o)
-    # clear colour where nothing was drawn
-    assert np.array_equal(rc[~cov_r], col[~cov_o])
-    dd = np.abs(rd.astype(np.int64) - dep.astype(np.int64))[cov_r]
-    assert dd.max() <= 128, dd.max()
     rel = np.max(np.abs(rc - col), axis=1) / np.maximum(np.max(np.abs(rc), axis=1), 1e-30)
-    rel = rel[cov_r]
-    assert np.mean(rel > 1e-3) <= 5e-3, np.mean(rel > 1e-3)
-    assert rel.max() <= 5e-2, rel.max()
+    bad = (rd != dep) | (rel > 1e-5)
+    assert bad.sum() <= 1e-4 * rd.size, (int(bad.sum()), rd.size)
+
+
+@pytest.mark.parametrize("name,disp", CASES)
+def test_oracle_grids_match_reference_dice_shade(built, name, disp):
+    """Position, pixel and depth grids bit for bit; quad colours within 1e-5
+    relative (the largest seen is 2e-7: the reference's shading goes through
+    the shim's vector operators, whose contraction gcc picks per call site)."""
+    oracle = _ref_lib()
+    if not hasattr(oracle.ref_pin(), "refk_dice_shade"):
+        pytest.skip("reference tree not compiled here")
+    sc, _, pid, rng = golden_case(name)
+    p = oracle.make_params(sc, displacement=disp)
+    sel = np.linspace(0, len(pid) - 1, min(len(pid), 160)).astype(int)
+    pid, rng = pid[sel], rng[sel]
+    rpos, rpxl, rdep, rcol, _ = oracle.ref_dice_shade(sc, 0, pid, rng, params=p)
+    written = 0
+    for k in range(len(pid)):
+        pos, pxl, dep = oracle.dice(sc, 0, pid[k], rng[k], params=p)
+        assert np.array_equal(rpos[k].view(np.uint32), pos.view(np.uint32)), k
+        assert np.array_equal(rpxl[k], pxl), k
+        assert np.array_equal(rdep[k].view(np.uint32), dep.view(np.uint32)), k
+        c = oracle.shade_quads(sc, 0, pid[k], rng[k], params=p)
+        w = ~np.isnan(rcol[k][:, 0])
+        written += int(w.sum())
+        rel = np.max(np.abs(rcol[k][w] - c[w]), axis=1) / np.maximum(np.max(np.abs(rcol[k][w]), axis=1), 1e-30)
+        assert rel.size == 0 or rel.max() <= 1e-5, (k, rel.max())
+    assert written > 0
 
 
 def test_reference_kernels_see_planted_oracle_change(built):
