@@ -84,13 +84,19 @@ __device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b)
 __device__ __forceinline__ float fdiv(float a, float b) { return __fdiv_rn(a, b); }
 
 // Packed pairs (the FFMA2 / FMUL2 / FADD2 instructions of sm_100 and later):
-// each component rounds exactly as ffma / fmul / fadd, one instruction issue
-// for two.  The kernels pack the x/y (and z/w) components of one evaluation.
+// each component rounds as ffma / fmul / fadd, one instruction issue for two.
+// The dice arithmetic packs the x/y and z/w components of one evaluation.
+// They are kept out of the bound-and-split arithmetic, which must not fuse:
+// there a packed product feeding a packed sum gave a different sub-patch set
+// than the scalar _rn operations (a contraction the -fmad=false build does
+// not rule out for the packed forms).  In the dice arithmetic a packed
+// product only feeds a multiply, the multiplicand of a fused multiply-add, or
+// (the viewport transform) an exact scaling by 0.5, where a contraction
+// could not change a bit.
 __device__ __forceinline__ float2 ffma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
 __device__ __forceinline__ float2 fmul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
 __device__ __forceinline__ float2 fadd2(float2 a, float2 b) { return __fadd2_rn(a, b); }
 __device__ __forceinline__ float2 dup2(float a) { return make_float2(a, a); }
-__device__ __forceinline__ float2 xy2(const F3& p) { return make_float2(p.x, p.y); }
 // src/base/utility.h:86-94
 __device__ __forceinline__ float minimum(float a, float b) { return a < b ? a : b; }
 __device__ __forceinline__ float maximum(float a, float b) { return a > b ? a : b; }
@@ -120,19 +126,18 @@ __device__ __forceinline__ F3 ld3(const float4* p) {
 }
 
 // glm 0.9.9 mat4 * vec4(p, 1): (m0*x + m1*y) + (m2*z + m3*1), per component.
-// Rows x and y as one packed pair, z alone.
 __device__ __forceinline__ F3 mv_point(const float* m, const F3& p) {
-    const float2 xy = fadd2(fadd2(fmul2(make_float2(m[0], m[1]), dup2(p.x)), fmul2(make_float2(m[4], m[5]), dup2(p.y))),
-                            fadd2(fmul2(make_float2(m[8], m[9]), dup2(p.z)), fmul2(make_float2(m[12], m[13]), dup2(1.0f))));
-    return F3{xy.x, xy.y, fadd(fadd(fmul(m[2], p.x), fmul(m[6], p.y)), fadd(fmul(m[10], p.z), fmul(m[14], 1.0f)))};
+    F3 r;
+    r.x = fadd(fadd(fmul(m[0], p.x), fmul(m[4], p.y)), fadd(fmul(m[8], p.z), fmul(m[12], 1.0f)));
+    r.y = fadd(fadd(fmul(m[1], p.x), fmul(m[5], p.y)), fadd(fmul(m[9], p.z), fmul(m[13], 1.0f)));
+    r.z = fadd(fadd(fmul(m[2], p.x), fmul(m[6], p.y)), fadd(fmul(m[10], p.z), fmul(m[14], 1.0f)));
+    return r;
 }
 
 // glm::distance: sqrt((dx*dx + dy*dy) + dz*dz)
 __device__ __forceinline__ float distance3(const F3& a, const F3& b) {
-    const float2 d = fadd2(xy2(b), make_float2(-a.x, -a.y));   // b - a, exactly as fsub
-    const float2 d2 = fmul2(d, d);
-    const float dz = fsub(b.z, a.z);
-    return __fsqrt_rn(fadd(fadd(d2.x, d2.y), fmul(dz, dz)));
+    float dx = fsub(b.x, a.x), dy = fsub(b.y, a.y), dz = fsub(b.z, a.z);
+    return __fsqrt_rn(fadd(fadd(fmul(dx, dx), fmul(dy, dy)), fmul(dz, dz)));
 }
 
 // Gregory patch (src/base/Patch.cpp:186-210), evaluated at (u, v) after the swap.
