@@ -85,8 +85,9 @@ typedef struct {
     int32_t bns_blocks;
     /* tuning knobs that do not change the image (0 = default):
      * raster_tile: tile of the depth|id key buffer in pixels (8, 16, 32);
-     * dice_group: sub-patches diced together per 256-thread block
-     * (8, 16 or 22 at reyes_patch_size 8; 2, 4 or 6 at 16) */
+     * dice_group: sub-patches diced together per block (8, 11, 16 or 22
+     * at reyes_patch_size 8; 2, 3, 4 or 6 at 16; 11 and 3 run 128-thread
+     * blocks, the others 256) */
     int32_t raster_tile;
     int32_t dice_group;
     /* bound-and-split criterion (mp_bound_criterion) */

@@ -3,10 +3,10 @@
 It picks, per workload shape, the values of the knobs that change speed but
 not the rendered sub-patch set:
 
-- ``dice_group``: sub-patches one fused 256-thread block claims from the
-  emitted sub-patch queue, dices, shades and rasterizes at a time (the queue
-  chunk of the dice/raster stage; 8, 16 or 22 for 8x8 dicing, 2, 4 or 6 for
-  16x16);
+- ``dice_group``: sub-patches one fused block claims from the emitted
+  sub-patch queue, dices, shades and rasterizes at a time (the queue chunk of
+  the dice/raster stage; 8, 11, 16 or 22 for 8x8 dicing, 2, 3, 4 or 6 for
+  16x16; 11 and 3 run 128-thread blocks, the others 256);
 - ``raster_tile``: the tile edge, in pixels, of the depth|id key buffer that
   the 64-bit atomicMin resolves visibility in (8, 16 or 32);
 - ``overlap``: bound-and-split and rasterization in one launch, with the
@@ -31,7 +31,8 @@ import os
 from dataclasses import dataclass, field
 from typing import Callable, Dict, Iterable, List, Optional
 
-GROUPS = {8: (8, 16, 22), 16: (2, 4, 6)}
+GROUPS = {8: (8, 11, 16, 22), 16: (2, 3, 4, 6)}
+DEFAULT_GROUP = {8: 11, 16: 6}   # the library's default dice_group per dice grid
 TILES = (8, 16, 32)
 OVERLAP = (False, True)
 CACHE_VERSION = 1
@@ -82,7 +83,7 @@ def candidates(patch_size: int = 8, tune_patch_size: bool = False,
     out = []
     for ps in sizes:
         gs = tuple(groups) if groups is not None else GROUPS[ps]
-        gs = tuple(sorted(gs, key=lambda g: g != GROUPS[ps][-1]))   # the default group first
+        gs = tuple(sorted(gs, key=lambda g: g != DEFAULT_GROUP[ps]))   # the default group first
         for g, t, ov in itertools.product(gs, tiles, overlap):
             c = {"dice_group": int(g), "raster_tile": int(t), "overlap": bool(ov)}
             if tune_patch_size:

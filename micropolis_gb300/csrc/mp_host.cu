@@ -649,10 +649,12 @@ mp_status mp_create(const mp_options* opts, mp_ctx** out) {
     if (o.bound_criterion != MP_BOUND_CPU && o.bound_criterion != MP_BOUND_GPU) return MP_ERR_INVALID_ARG;
     if (o.raster_tile == 0) o.raster_tile = 8;
     if (o.raster_tile != 8 && o.raster_tile != 16 && o.raster_tile != 32) return MP_ERR_INVALID_ARG;
-    if (o.dice_group == 0) o.dice_group = o.reyes_patch_size == 16 ? 6 : 22;
-    if (o.reyes_patch_size == 8 && o.dice_group != 8 && o.dice_group != 16 && o.dice_group != 22)
+    if (o.dice_group == 0) o.dice_group = o.reyes_patch_size == 16 ? 6 : 11;
+    if (o.reyes_patch_size == 8 && o.dice_group != 8 && o.dice_group != 11 && o.dice_group != 16 &&
+        o.dice_group != 22)
         return MP_ERR_INVALID_ARG;
-    if (o.reyes_patch_size == 16 && o.dice_group != 2 && o.dice_group != 4 && o.dice_group != 6)
+    if (o.reyes_patch_size == 16 && o.dice_group != 2 && o.dice_group != 3 && o.dice_group != 4 &&
+        o.dice_group != 6)
         return MP_ERR_INVALID_ARG;
     mp_ctx* c = new mp_ctx();
     c->opt = o;

@@ -151,13 +151,18 @@ __device__ __forceinline__ void push_big(BigQuad* big, long long big_cap, unsign
     big[i] = b;
 }
 
-// The fused kernel works on groups of NS sub-patches per 256-thread block:
+// The fused kernel works on groups of NS sub-patches per block:
 // NS * (PS+1)^2 dice vertices are spread over all threads (22 * 81 = 1782 =
 // 7 rounds of 256 at PS = 8), then the block bounds, then one thread per quad
 // that can touch a pixel.  The inputs of the next group (sub-patch records,
 // control points, matrices) are copied into the other half of a double
 // buffer with cp.async while the current group is diced and rasterized.
-constexpr int kFusedThreads = 256;
+// Groups of 11 (PS = 8) and 3 (PS = 16) run half-size blocks of 128 threads,
+// twice as many per SM, the others 256.
+template <int NS>
+constexpr int fused_threads() {
+    return (NS == 11 || NS == 3) ? 128 : 256;
+}
 
 static_assert(offsetof(DrawDev, proj) == offsetof(DrawDev, mv) + 16 * sizeof(float), "mv, proj adjacent");
 static_assert(offsetof(DrawDev, mv) % 16 == 0 && sizeof(DrawDev) % 16 == 0, "16-byte copies of mv/proj");
@@ -176,16 +181,16 @@ template <int PS, int NS_>
 struct FusedSmem {
     static constexpr int NS = NS_, G = PS + 1, NV = G * G, NB = (PS / 8) * (PS / 8);
     GroupStage<NS> st[2];
-    int bound[NS][NB][4];
-    int tiles[NS][NB][4];     // block tile range; tiles[k][b][0] > tiles[k][b][2] marks a skipped block
-    unsigned zero[NS];
-    unsigned n_live;
+    // per group state, double-buffered with st: block bounds, blocks with a
+    // vertex at eye z == 0, and the number of listed quads
+    int bound[2][NS][NB][4];
+    unsigned zero[2][NS];
+    unsigned n_live[2];
     unsigned short live[NS * PS * PS];   // quads that may touch a pixel, in bound-phase order
     float tx[NS][G], ty[NS][G];
     float4 vw[NS][G], cw[NS][G];
-    int px[NS * NV], py[NS * NV];
-    float dep[NS * NV];
-    float ex[NS * NV], ey[NS * NV], ez[NS * NV];
+    float4 edep[NS * NV];     // eye position and NDC depth of each dice vertex
+    int2 pxy[NS * NV];        // fixed-point pixel coordinates
 };
 
 __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
@@ -205,7 +210,7 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 // control points, matrices, type and view (asynchronous; the caller waits).
 template <int NS>
 __device__ __forceinline__ void stage_inputs(GroupStage<NS>& st, int n, const DrawDev* __restrict__ draws) {
-    for (int i = threadIdx.x; i < n * 32; i += kFusedThreads) {
+    for (int i = threadIdx.x; i < n * 32; i += fused_threads<NS>()) {
         const int k = i >> 5, c = i & 31;
         const int2 m = st.meta[k];
         const DrawDev* d = draws + m.y;
@@ -223,25 +228,59 @@ __device__ __forceinline__ void stage_inputs(GroupStage<NS>& st, int n, const Dr
     cp_async_commit();
 }
 
-// Stages the group [base, base + n) into st from scratch (records, then
-// inputs) and waits for it; ends with a barrier.
-template <int NS>
-__device__ __forceinline__ void stage_group(GroupStage<NS>& st, long long base, int n, const SubPatches& sub,
-                                            const DrawDev* __restrict__ draws) {
+// Prepares the state of a group of n sub-patches whose records are in
+// sm.st[b]: the dice parameters and Bernstein weights of each row / column of
+// vertices, reset block bounds (viewport max, 0), eye-plane flags and listed
+// quad count.  This thread takes the items first, first + threads, ...
+template <int PS, int NS>
+__device__ __forceinline__ void prepare_group(FusedSmem<PS, NS>& sm, int b, int n, const FrameDev& fr, int first) {
+    constexpr int G = PS + 1, NB = (PS / 8) * (PS / 8);
+    const GroupStage<NS>& st = sm.st[b];
+    for (int i = first; i < n * 2 * G; i += fused_threads<NS>()) {
+        const int k = i / (2 * G), c = i % (2 * G);
+        const float4 rg = st.range[k];
+        if (c < G) {
+            const float t = dice_param(rg.x, rg.z, c, fr);
+            sm.tx[k][c] = t;
+            sm.vw[k][c] = row_weights(t);
+        } else {
+            const float t = dice_param(rg.y, rg.w, c - G, fr);
+            sm.ty[k][c - G] = t;
+            sm.cw[k][c - G] = col_weights(t);
+        }
+    }
+    const int vmaxx = (fr.W << fr.shift) - 1, vmaxy = (fr.H << fr.shift) - 1;
+    for (int i = first; i < n * NB; i += fused_threads<NS>()) {
+        int* bb = sm.bound[b][i / NB][i % NB];
+        bb[0] = vmaxx; bb[1] = vmaxy; bb[2] = 0; bb[3] = 0;
+    }
+    if (first < n) sm.zero[b][first] = 0;
+    if (first == 0) sm.n_live[b] = 0;
+}
+
+// Stages the group [base, base + n) into sm.st[0] from scratch (records,
+// then inputs) and prepares it; ends with a barrier.
+template <int PS, int NS>
+__device__ __forceinline__ void stage_group(FusedSmem<PS, NS>& sm, long long base, int n, const SubPatches& sub,
+                                            const DrawDev* __restrict__ draws, const FrameDev& fr) {
+    GroupStage<NS>& st = sm.st[0];
     if ((int)threadIdx.x < n) {
         st.range[threadIdx.x] = sub.range[base + threadIdx.x];
         st.meta[threadIdx.x] = sub.meta[base + threadIdx.x];
     }
     __syncthreads();
     stage_inputs(st, n, draws);
+    prepare_group(sm, 0, n, fr, threadIdx.x);
     cp_async_wait_all();
     __syncthreads();
 }
 
 // Dices, shades and rasterizes the n (<= NS) sub-patches at [base, base+n)
-// of the emitted list, whose inputs are staged in sm.st[b], with the whole
-// block; meanwhile stages the n_next sub-patches at next_base into
-// sm.st[b ^ 1].  Ends with a barrier after which both are complete.
+// of the emitted list, whose inputs are staged and prepared in buffer b, with
+// the whole block; meanwhile stages and prepares the n_next sub-patches at
+// next_base in buffer b ^ 1.  Three phases (dice; block bounds and the list
+// of quads that can touch a pixel; raster), each ending with a barrier after
+// which both groups' buffers are complete.
 template <int PS, int NS>
 __device__ __forceinline__ void raster_group(FusedSmem<PS, NS>& sm, int b, long long base, int n,
                                              long long next_base, int n_next, const DrawDev* __restrict__ draws,
@@ -249,7 +288,7 @@ __device__ __forceinline__ void raster_group(FusedSmem<PS, NS>& sm, int b, long 
                                              float* __restrict__ mshade, BigQuad* big, long long big_cap,
                                              unsigned long long* ctrl, const V3& light, long long& frags) {
     using SM = FusedSmem<PS, NS>;
-    constexpr int G = SM::G, NV = SM::NV, NQ = PS * PS, BPL = PS / 8, NB = SM::NB;
+    constexpr int G = SM::G, NV = SM::NV, NQ = PS * PS, BPL = PS / 8, NB = SM::NB, TH = fused_threads<NS>();
     GroupStage<NS>& cur = sm.st[b];
     GroupStage<NS>& nxt = sm.st[b ^ 1];
     const int tid = threadIdx.x, lane = tid & 31;
@@ -262,29 +301,8 @@ __device__ __forceinline__ void raster_group(FusedSmem<PS, NS>& sm, int b, long 
         next_range = sub.range[next_base + tid];
         next_meta = sub.meta[next_base + tid];
     }
-    if (tid < n) sm.zero[tid] = 0;
-    if (tid == 0) sm.n_live = 0;
-    for (int i = tid; i < n * NB; i += kFusedThreads) {
-        int* bb = sm.bound[i / NB][i % NB];
-        bb[0] = vmaxx; bb[1] = vmaxy; bb[2] = 0; bb[3] = 0;
-    }
-    // dice parameters and Bernstein weights of each row / column of vertices
-    for (int i = tid; i < n * 2 * G; i += kFusedThreads) {
-        const int k = i / (2 * G), c = i % (2 * G);
-        const float4 rg = cur.range[k];
-        if (c < G) {
-            const float t = dice_param(rg.x, rg.z, c, fr);
-            sm.tx[k][c] = t;
-            sm.vw[k][c] = row_weights(t);
-        } else {
-            const float t = dice_param(rg.y, rg.w, c - G, fr);
-            sm.ty[k][c - G] = t;
-            sm.cw[k][c - G] = col_weights(t);
-        }
-    }
-    __syncthreads();
     // dice vertices (kernels/dice.cl:37-80)
-    for (int i = tid; i < n * NV; i += kFusedThreads) {
+    for (int i = tid; i < n * NV; i += TH) {
         const int k = i / NV, v = i % NV;
         const int nu = v % G, nv = v / G;
         const float* mvp = cur.mvp[k];
@@ -293,18 +311,14 @@ __device__ __forceinline__ void raster_group(FusedSmem<PS, NS>& sm, int b, long 
         int px, py;
         float dep;
         project_vertex_m(mvp + 16, fr, pos, px, py, dep);
-        sm.px[i] = px;
-        sm.py[i] = py;
-        sm.dep[i] = dep;
-        sm.ex[i] = pos.x;
-        sm.ey[i] = pos.y;
-        sm.ez[i] = pos.z;
+        sm.pxy[i] = make_int2(px, py);
+        sm.edep[i] = make_float4(pos.x, pos.y, pos.z, dep);
         if (pos.z == 0.0f) {
             // a vertex at eye z == 0 drops every 8x8 block it belongs to (kernels/reyes.cl:130-162)
             unsigned zb = 0;
             for (int bv = max(nv - 1, 0) / 8; bv <= min(nv, PS - 1) / 8; ++bv)
                 for (int bu = max(nu - 1, 0) / 8; bu <= min(nu, PS - 1) / 8; ++bu) zb |= 1u << (bu + bv * BPL);
-            atomicOr(&sm.zero[k], zb);
+            atomicOr(&sm.zero[b][k], zb);
         }
     }
     if (tid < n_next) {
@@ -319,11 +333,12 @@ __device__ __forceinline__ void raster_group(FusedSmem<PS, NS>& sm, int b, long 
     // n * NQ is a multiple of 32, so whole warps run each round; the quads of
     // one warp share a sub-patch, and their 8x8 blocks are fixed by the lane:
     // one block at PS = 8, and at PS = 16 two, lanes with bit 3 clear / set.
-    for (int i = tid; i < n * NQ; i += kFusedThreads) {
+    for (int i = tid; i < n * NQ; i += TH) {
         const int k = i / NQ, q = i % NQ;
         const int nu = q % PS, nv = q / PS, i0 = k * NV + nu + nv * G;
-        const int qx[4] = {sm.px[i0], sm.px[i0 + 1], sm.px[i0 + G], sm.px[i0 + G + 1]};
-        const int qy[4] = {sm.py[i0], sm.py[i0 + 1], sm.py[i0 + G], sm.py[i0 + G + 1]};
+        const int2 c0 = sm.pxy[i0], c1 = sm.pxy[i0 + 1], c2 = sm.pxy[i0 + G], c3 = sm.pxy[i0 + G + 1];
+        const int qx[4] = {c0.x, c1.x, c2.x, c3.x};
+        const int qy[4] = {c0.y, c1.y, c2.y, c3.y};
         const int minx = min(min(qx[0], qx[1]), min(qx[2], qx[3]));
         const int maxx = max(max(qx[0], qx[1]), max(qx[2], qx[3]));
         const int miny = min(min(qy[0], qy[1]), min(qy[2], qy[3]));
@@ -339,7 +354,7 @@ __device__ __forceinline__ void raster_group(FusedSmem<PS, NS>& sm, int b, long 
         const bool live = !fast || (wind && quad_pixels(fr, minx, miny, maxx, maxy, x0, y0, x1, y1));
         const unsigned lm = __ballot_sync(0xffffffffu, live);
         unsigned at = 0;
-        if (lane == 0 && lm) at = atomicAdd(&sm.n_live, (unsigned)__popc(lm));
+        if (lane == 0 && lm) at = atomicAdd(&sm.n_live[b], (unsigned)__popc(lm));
         at = __shfl_sync(0xffffffffu, at, 0);
         if (live) sm.live[at + __popc(lm & lanemask_lt())] = (unsigned short)i;
         // the block bound starts at (viewport max, 0) and takes front-facing quads
@@ -350,7 +365,7 @@ __device__ __forceinline__ void raster_group(FusedSmem<PS, NS>& sm, int b, long 
         const int bx1 = __reduce_max_sync(grp, ff ? max(0, maxx) : 0);
         const int by1 = __reduce_max_sync(grp, ff ? max(0, maxy) : 0);
         if ((lane & (PS == 8 ? 31 : 23)) == 0) {
-            int* bb = sm.bound[k][(nu >> 3) + (nv >> 3) * BPL];
+            int* bb = sm.bound[b][k][(nu >> 3) + (nv >> 3) * BPL];
             atomicMin(bb + 0, bx0);
             atomicMin(bb + 1, by0);
             atomicMax(bb + 2, bx1);
@@ -358,35 +373,31 @@ __device__ __forceinline__ void raster_group(FusedSmem<PS, NS>& sm, int b, long 
         }
     }
     __syncthreads();
-    // the tile range of each block, or a skip mark
-    for (int i = tid; i < n * NB; i += kFusedThreads) {
-        const int k = i / NB, bk = i % NB;
-        const int* bb = sm.bound[k][bk];
-        int* t = sm.tiles[k][bk];
-        if (!block_tiles(fr, bb[0], bb[1], bb[2], bb[3], !((sm.zero[k] >> bk) & 1), t)) {
-            t[0] = 1;
-            t[2] = 0;
-        }
-    }
-    __syncthreads();
+    // the next group's weights and state, from the highest thread down (the
+    // raster below occupies the lowest threads)
+    prepare_group(sm, b ^ 1, n_next, fr, TH - 1 - tid);
     // rasterize the listed quads of live blocks
-    const int n_live = (int)sm.n_live;
-    for (int j = tid; j < n_live; j += kFusedThreads) {
+    const int n_live = (int)sm.n_live[b];
+    for (int j = tid; j < n_live; j += TH) {
         const int i = sm.live[j];
         const int k = i / NQ, q = i % NQ;
         const int nu = q % PS, nv = q / PS, blk = (nu >> 3) + (nv >> 3) * BPL;
-        const int* tp = sm.tiles[k][blk];
-        if (tp[0] > tp[2]) continue;
-        const int tiles[4] = {tp[0], tp[1], tp[2], tp[3]};
+        // the block's tile range, or skip it (clamp, eye-plane flag, is_empty)
+        const int* bb = sm.bound[b][k][blk];
+        int tiles[4];
+        if (!block_tiles(fr, bb[0], bb[1], bb[2], bb[3], !((sm.zero[b][k] >> blk) & 1), tiles)) continue;
         const int i0 = k * NV + nu + nv * G;
         const int idx[4] = {i0, i0 + 1, i0 + G, i0 + G + 1};
         int qx[4], qy[4];
         float qd[4];
+        float4 e[4];
 #pragma unroll
         for (int c = 0; c < 4; ++c) {
-            qx[c] = sm.px[idx[c]];
-            qy[c] = sm.py[idx[c]];
-            qd[c] = sm.dep[idx[c]];
+            const int2 q = sm.pxy[idx[c]];
+            e[c] = sm.edep[idx[c]];
+            qx[c] = q.x;
+            qy[c] = q.y;
+            qd[c] = e[c].w;
         }
         const long long s = base + k;
         const unsigned mp_id = (unsigned)(s * NQ + nu + nv * PS);
@@ -401,9 +412,8 @@ __device__ __forceinline__ void raster_group(FusedSmem<PS, NS>& sm, int b, long 
         if (f > 0 || !fast) {
             // the diffuse factor of a quad that may own pixels; resolve
             // turns it into the colour of kernels/reyes.cl:191
-            mshade[mp_id] = shade_m_l(light, sm.ex[idx[0]], sm.ey[idx[0]], sm.ez[idx[0]], sm.ex[idx[1]], sm.ey[idx[1]],
-                                    sm.ez[idx[1]], sm.ex[idx[2]], sm.ey[idx[2]], sm.ez[idx[2]], sm.ex[idx[3]],
-                                    sm.ey[idx[3]], sm.ez[idx[3]]);
+            mshade[mp_id] = shade_m_l(light, e[0].x, e[0].y, e[0].z, e[1].x, e[1].y, e[1].z, e[2].x, e[2].y, e[2].z,
+                                      e[3].x, e[3].y, e[3].z);
         }
         frags += f;
     }
@@ -412,7 +422,7 @@ __device__ __forceinline__ void raster_group(FusedSmem<PS, NS>& sm, int b, long 
 }
 
 template <int PS, int NS>
-__global__ void __launch_bounds__(kFusedThreads, 3)
+__global__ void __launch_bounds__(fused_threads<NS>(), 768 / fused_threads<NS>())
     raster_fused_kernel(const DrawDev* __restrict__ draws, FrameDev fr, SubPatches sub, Framebuffer fb,
                         float* __restrict__ mshade, BigQuad* big, long long big_cap, unsigned long long* ctrl) {
     using SM = FusedSmem<PS, NS>;
@@ -424,7 +434,7 @@ __global__ void __launch_bounds__(kFusedThreads, 3)
     long long frags = 0;
     const long long stride = (long long)gridDim.x * NS;
     long long base = (long long)blockIdx.x * NS;
-    if (base < S) stage_group(sm.st[0], base, (int)min((long long)NS, S - base), sub, draws);
+    if (base < S) stage_group(sm, base, (int)min((long long)NS, S - base), sub, draws, fr);
     for (int b = 0; base < S; base += stride, b ^= 1) {
         const long long next = base + stride;
         raster_group<PS, NS>(sm, b, base, (int)min((long long)NS, S - base), next,
@@ -449,13 +459,13 @@ constexpr int kFrameStagedDraws = 64;
 constexpr size_t kFramePtsOffset = (kFrameStagedDraws * sizeof(DrawDev) + 15) / 16 * 16;
 template <int PS, int NS>
 constexpr size_t frame_smem() {
-    return sizeof(FusedSmem<PS, NS>) > kFramePtsOffset + 27 * kFusedThreads * sizeof(float)
+    return sizeof(FusedSmem<PS, NS>) > kFramePtsOffset + 27 * fused_threads<NS>() * sizeof(float)
                ? sizeof(FusedSmem<PS, NS>)
-               : kFramePtsOffset + 27 * kFusedThreads * sizeof(float);
+               : kFramePtsOffset + 27 * fused_threads<NS>() * sizeof(float);
 }
 
 template <int PS, int NS>
-__global__ void __launch_bounds__(kFusedThreads, 3)
+__global__ void __launch_bounds__(fused_threads<NS>(), 768 / fused_threads<NS>())
     frame_kernel(const DrawDev* __restrict__ gdraws, const int* __restrict__ root_prefix, int n_draws, FrameDev fr,
                  Queue q, SubPatches sub, Framebuffer fb, float* __restrict__ mshade, BigQuad* big, long long big_cap,
                  unsigned long long* ctrl, long long spin_limit, int n_bns_ctas) {
@@ -478,7 +488,7 @@ __global__ void __launch_bounds__(kFusedThreads, 3)
         }
         // the CPU criterion only: the host runs the GPU criterion as two launches
         float* pts = reinterpret_cast<float*>(smem_raw + kPtsOffset);
-        bns_warp_loop<0, kFusedThreads>(staged ? sd : gdraws, root_prefix, n_draws, fr, q, sub, sub.seq, ctrl,
+        bns_warp_loop<0, fused_threads<NS>()>(staged ? sd : gdraws, root_prefix, n_draws, fr, q, sub, sub.seq, ctrl,
                                         spin_limit, pts);
         __syncthreads();
     }
@@ -516,7 +526,7 @@ __global__ void __launch_bounds__(kFusedThreads, 3)
         }
         const int n = __syncthreads_count(ready);
         if (n == 0 || __syncthreads_or(gave_up)) break;
-        stage_group(sm.st[0], base, n, sub, gdraws);
+        stage_group(sm, base, n, sub, gdraws, fr);
         raster_group<PS, NS>(sm, 0, base, n, 0, 0, gdraws, fr, sub, fb, mshade, big, big_cap, ctrl, light, frags);
     }
     frags = __reduce_add_sync(0xffffffffu, (unsigned)frags);
@@ -801,12 +811,12 @@ __global__ void atomic_bench_kernel(unsigned long long* buf, long long n_slots, 
 }
 
 template <typename K>
-int resident_grid(K kernel, size_t smem) {
+int resident_grid(K kernel, size_t smem, int threads) {
     int dev = 0, sms = 0, per_sm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kFusedThreads, smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem);
     if (per_sm < 1) per_sm = 1;
     return sms * per_sm;
 }
@@ -820,10 +830,12 @@ template <typename F>
 void dispatch_group(int PS, int group, F&& f) {
     if (PS == 16) {
         if (group == 2) f(Tag<16, 2>{});
+        else if (group == 3) f(Tag<16, 3>{});
         else if (group == 4) f(Tag<16, 4>{});
         else f(Tag<16, 6>{});
     } else {
         if (group == 8) f(Tag<8, 8>{});
+        else if (group == 11) f(Tag<8, 11>{});
         else if (group == 16) f(Tag<8, 16>{});
         else f(Tag<8, 22>{});
     }
@@ -849,7 +861,8 @@ int raster_fused_grid(int PS, int group) {
     int g = 0;
     dispatch_group(PS, group, [&](auto t) {
         using T = decltype(t);
-        g = resident_grid(raster_fused_kernel<T::ps, T::ns>, sizeof(FusedSmem<T::ps, T::ns>));
+        g = resident_grid(raster_fused_kernel<T::ps, T::ns>, sizeof(FusedSmem<T::ps, T::ns>),
+                          fused_threads<T::ns>());
     });
     return g;
 }
@@ -859,7 +872,7 @@ void launch_raster_fused(const DrawDev* draws, const FrameDev& fr, const SubPatc
                          cudaStream_t s) {
     dispatch_group(fr.PS, group, [&](auto t) {
         using T = decltype(t);
-        raster_fused_kernel<T::ps, T::ns><<<grid, kFusedThreads, sizeof(FusedSmem<T::ps, T::ns>), s>>>(
+        raster_fused_kernel<T::ps, T::ns><<<grid, fused_threads<T::ns>(), sizeof(FusedSmem<T::ps, T::ns>), s>>>(
             draws, fr, sub, fb, mshade, big, big_cap, ctrl);
     });
 }
@@ -868,7 +881,7 @@ int frame_kernel_grid(int PS, int group) {
     int g = 0;
     dispatch_group(PS, group, [&](auto t) {
         using T = decltype(t);
-        g = resident_grid(frame_kernel<T::ps, T::ns>, frame_smem<T::ps, T::ns>());
+        g = resident_grid(frame_kernel<T::ps, T::ns>, frame_smem<T::ps, T::ns>(), fused_threads<T::ns>());
     });
     return g;
 }
@@ -879,7 +892,7 @@ void launch_frame_kernel(const DrawDev* draws, const int* root_prefix, int n_dra
                          cudaStream_t s) {
     dispatch_group(fr.PS, group, [&](auto t) {
         using T = decltype(t);
-        frame_kernel<T::ps, T::ns><<<grid, kFusedThreads, frame_smem<T::ps, T::ns>(), s>>>(
+        frame_kernel<T::ps, T::ns><<<grid, fused_threads<T::ns>(), frame_smem<T::ps, T::ns>(), s>>>(
             draws, root_prefix, n_draws, fr, q, sub, fb, mshade, big, big_cap, ctrl, spin_limit, n_bns_ctas);
     });
 }

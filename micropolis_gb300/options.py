@@ -35,7 +35,7 @@ class ReyesOptions:
     overlap: bool = False                      # batched: rasterize while bound-and-split emits
     bns_blocks: int = 0                        # batched overlap: blocks starting with bound-and-split (0 = auto)
     raster_tile: int = 0                       # depth|id key buffer tile in pixels (0 = 8)
-    dice_group: int = 0                        # sub-patches per fused 256-thread block (0 = default)
+    dice_group: int = 0                        # sub-patches per fused block (0 = default)
     bound_criterion: int = 0                   # 0: the reference's CPU criterion, 1: its GPU criterion
 
     def update(self, **kw) -> "ReyesOptions":

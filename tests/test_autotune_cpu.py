@@ -13,13 +13,13 @@ def _scene(n=64, **kw):
 
 def test_candidates_cover_space_default_first():
     c8 = autotune.candidates(8)
-    assert len(c8) == 3 * 3 * 2
-    assert c8[0] == {"dice_group": 22, "raster_tile": 8, "overlap": False}
-    assert {c["dice_group"] for c in c8} == {8, 16, 22}
+    assert len(c8) == 4 * 3 * 2
+    assert c8[0] == {"dice_group": 11, "raster_tile": 8, "overlap": False}
+    assert {c["dice_group"] for c in c8} == {8, 11, 16, 22}
     c16 = autotune.candidates(16)
-    assert {c["dice_group"] for c in c16} == {2, 4, 6}
+    assert {c["dice_group"] for c in c16} == {2, 3, 4, 6}
     both = autotune.candidates(8, tune_patch_size=True)
-    assert len(both) == 36 and {c["reyes_patch_size"] for c in both} == {8, 16}
+    assert len(both) == 48 and {c["reyes_patch_size"] for c in both} == {8, 16}
 
 
 def test_choose_by_time_and_by_rate():
@@ -58,14 +58,14 @@ def test_tune_picks_fastest_and_caches(tmp_path):
 
     r = autotune.tune(sc, cache=cache, measure=fake, device="dev")
     assert r.best == {"dice_group": 8, "raster_tile": 16, "overlap": True}
-    assert not r.cached and len(calls) == 18 and len(r.trials) == 18
+    assert not r.cached and len(calls) == 24 and len(r.trials) == 24
     data = json.load(open(cache))
     assert data["version"] == autotune.CACHE_VERSION and r.key in data
     r2 = autotune.tune(sc, cache=cache, measure=fake, device="dev")
-    assert r2.cached and r2.best == r.best and len(calls) == 18
+    assert r2.cached and r2.best == r.best and len(calls) == 24
     # another device tunes again
     autotune.tune(sc, cache=cache, measure=fake, device="other")
-    assert len(calls) == 36
+    assert len(calls) == 48
 
 
 def test_tune_patch_size_scores_rate(tmp_path):

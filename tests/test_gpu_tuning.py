@@ -30,7 +30,7 @@ def _oracle(sc):
     return want, col, dep, st
 
 
-@pytest.mark.parametrize("ps,groups", [(8, (8, 16, 22)), (16, (2, 4, 6))])
+@pytest.mark.parametrize("ps,groups", [(8, (8, 11, 16, 22)), (16, (2, 3, 4, 6))])
 def test_knobs_match_oracle(built, cuda, ps, groups):
     from micropolis_gb300.renderer import render_scene, renderer_for
     sc = _scene(ps)
@@ -68,7 +68,7 @@ def test_autotuner_on_gpu(built, cuda, tmp_path):
     sc = _scene(8)
     cache = str(tmp_path / "tune.json")
     res = autotune.tune(sc, frames=2, warmup=1, cache=cache)
-    assert len(res.trials) == 18 and all(t.ms > 0 for t in res.trials)
+    assert len(res.trials) == 24 and all(t.ms > 0 for t in res.trials)
     assert len({t.micropolygons for t in res.trials}) == 1
     assert autotune.tune(sc, cache=cache).cached
     r = autotune.tuned_renderer(sc, cache=cache)
