@@ -24,6 +24,13 @@ __device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long
 __device__ __forceinline__ void st_release_u64(unsigned long long* p, unsigned long long v) {
     asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
+// A release fence followed by relaxed stores: each store publishes every
+// write this thread made before the fence (the PTX release pattern), so two
+// flags need one fence.
+__device__ __forceinline__ void fence_acq_rel_gpu() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
+__device__ __forceinline__ void st_relaxed_u32(unsigned* p, unsigned v) {
+    asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
 __device__ __forceinline__ unsigned lanemask_lt() {
     unsigned m;
     asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
@@ -175,9 +182,10 @@ __device__ __forceinline__ void bns_warp_loop(const DrawDev* draws, const int* _
                     store_inherited(q.pts + s0 * kPtsPerSlot, dec, 0, depth + 1, sp, st);
                     store_inherited(q.pts + (s0 + 1) * kPtsPerSlot, dec, 1, depth + 1, sp, st);
                 }
-                // release: the item stores above are visible before the slot's epoch
-                st_release_u32(q.seq + s0, epoch);
-                st_release_u32(q.seq + s0 + 1, epoch);
+                // release: the item stores above are visible before the slots' epochs
+                fence_acq_rel_gpu();
+                st_relaxed_u32(q.seq + s0, epoch);
+                st_relaxed_u32(q.seq + s0 + 1, epoch);
             } else {
                 set_status(ctrl, kErrOverflow);
             }
