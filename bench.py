@@ -41,12 +41,12 @@ L2_FLUSH_BYTES = 256 << 20
 # profiles/bns_persistent_mixed4096_1920x1080.md and
 # profiles/resolve_mixed4096_1920x1080.md).  ncu replays with cold
 # caches, so these are upper bounds for a launch inside a frame.
-NCU_TRAFFIC = {"dice_raster": 101_992_192 + 65_780_480, "bound_split": 2_746_624 + 200_429_824,
+NCU_TRAFFIC = {"dice_raster": 101_992_192 + 65_780_480, "bound_split": 2_698_240 + 200_370_944,
                "resolve_or_shade": 62_738_688 + 8_585_472}
 # Warp instructions per launch (smsp__inst_executed.sum) from the same
 # captures: the dice+raster kernel is bound by instruction issue, whose peak
 # is 4 warp instructions per SM per cycle.
-NCU_INST = {"dice_raster": 1_068_466_194, "bound_split": 169_990_039}
+NCU_INST = {"dice_raster": 1_068_466_194, "bound_split": 161_999_590}
 
 
 def parse():
