@@ -301,10 +301,11 @@ __device__ __forceinline__ void raster_group(FusedSmem<PS, NS>& sm, int b, long 
         next_range = sub.range[next_base + tid];
         next_meta = sub.meta[next_base + tid];
     }
-    // dice vertices (kernels/dice.cl:37-80)
+    // dice vertices (kernels/dice.cl:37-80); vertex i is (k, nu, nv) with
+    // i = k * NV + nv * G + nu, stepped by TH without divisions
+    constexpr int DK = TH / NV, DNV = (TH % NV) / G, DNU = (TH % NV) % G;
+    int k = tid / NV, nv = (tid % NV) / G, nu = (tid % NV) % G;
     for (int i = tid; i < n * NV; i += TH) {
-        const int k = i / NV, v = i % NV;
-        const int nu = v % G, nv = v / G;
         const float* mvp = cur.mvp[k];
         float4 pos = dice_eye_w(cur.tv[k][0], mvp, fr, cur.cp[k], sm.tx[k][nu], sm.ty[k][nv], sm.vw[k][nu],
                                 sm.cw[k][nv]);
@@ -320,6 +321,11 @@ __device__ __forceinline__ void raster_group(FusedSmem<PS, NS>& sm, int b, long 
                 for (int bu = max(nu - 1, 0) / 8; bu <= min(nu, PS - 1) / 8; ++bu) zb |= 1u << (bu + bv * BPL);
             atomicOr(&sm.zero[b][k], zb);
         }
+        k += DK;
+        nv += DNV;
+        nu += DNU;
+        if (nu >= G) { nu -= G; ++nv; }
+        if (nv >= G) { nv -= G; ++k; }
     }
     if (tid < n_next) {
         nxt.range[tid] = next_range;
