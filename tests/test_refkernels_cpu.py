@@ -21,6 +21,12 @@ EMPTY = 0x7fffffff
 CASES = [("heightfield_1024x768", 0), ("heightfield_1024x768", 1), ("mixed96_bezier_512", 0),
          ("mixed96_gregory_512", 0), ("mixed96_gregory_512", 1), ("mixed96_gregory_depth3_512", 1),
          ("heightfield_eye_plane_512x384", 0)]
+# 16x16 dicing (four 8x8 blocks per sub-patch), no backface culling, 4 subpixel bits
+FRAME_CASES = [(n, d, {}) for n, d in CASES] + [
+    ("mixed96_bezier_512", 0, {"reyes_patch_size": 16}),
+    ("heightfield_eye_plane_512x384", 1, {"reyes_patch_size": 16}),
+    ("mixed96_gregory_512", 0, {"backface_culling": 0, "reyes_patch_size": 16}),
+    ("heightfield_1024x768", 0, {"subpixel_bits": 4})]
 
 
 def _ref_lib():
@@ -31,11 +37,11 @@ def _ref_lib():
     return oracle
 
 
-@pytest.mark.parametrize("name,disp", CASES)
-def test_oracle_frame_matches_reference_kernels(built, name, disp):
+@pytest.mark.parametrize("name,disp,over", FRAME_CASES)
+def test_oracle_frame_matches_reference_kernels(built, name, disp, over):
     oracle = _ref_lib()
     sc, _, _, _ = golden_case(name)
-    p = oracle.make_params(sc, displacement=disp)
+    p = oracle.make_params(sc, displacement=disp, **over)
     rc, rd, rn = oracle.ref_render(sc, params=p)
     col, dep, st = oracle.render(sc, params=p)
     assert rn == st["subpatches"]
