@@ -408,7 +408,7 @@ def main():
                for d in sc.draws]
     col_host = torch.empty((W * H, 4), dtype=torch.float32).pin_memory().numpy()
     dep_host = torch.empty((W * H,), dtype=torch.int32).pin_memory().numpy()
-    h2d = sum(int(c.shape[0] * c.shape[1]) * 16 for c in host_cp)
+    h2d = sum(int(c.nbytes) for c in host_cp)          # xyz, widened to (x, y, z, 1) on the device
     d2h = W * H * 16 + W * H * 4
 
     def e2e_step():

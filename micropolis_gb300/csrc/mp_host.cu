@@ -96,8 +96,10 @@ struct mp_ctx {
     int bns_grid = 0, raster_grid = 0, frame_grid = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     bool stage_timing = false;
-    void* staging = nullptr;          // pinned upload buffer
+    void* staging = nullptr;          // pinned upload buffer (xyz of pageable sources)
     size_t staging_bytes = 0;
+    float* xyz_dev = nullptr;         // uploaded xyz before widening to (x, y, z, 1)
+    size_t xyz_cap = 0;               // floats
     cudaEvent_t sev[8] = {};
     mp_stats stats{};
     long long plain_bounds = 0, plain_passes = 0, plain_out = 0, plain_kernels = 0;
@@ -729,6 +731,7 @@ void mp_destroy(mp_ctx* c) {
     dfree(c->ctrl);
     if (c->h_ctrl) cudaFreeHost(c->h_ctrl);
     if (c->staging) cudaFreeHost(c->staging);
+    dfree(c->xyz_dev);
     dfree(c->d_draws);
     dfree(c->d_root_prefix);
     if (c->h_draws) cudaFreeHost(c->h_draws);
@@ -798,22 +801,42 @@ static mp_status load_common(mp_ctx* c, uint64_t handle, const void* src, size_t
         if (device) {
             CK(cudaMemcpyAsync(m.cp, src, sizeof(float4) * n_points, cudaMemcpyDeviceToDevice, c->stream));
         } else {
-            // src/Reyes/PatchIndex.cpp:83-98: widen vec3 to (x, y, z, 1) and upload,
-            // through a pinned staging buffer reused across loads
-            if (c->staging_bytes < sizeof(float4) * n_points) {
+            // src/Reyes/PatchIndex.cpp:83-98: upload the vec3 data and widen it
+            // to (x, y, z, 1) on the device.  Page-locked sources are copied
+            // directly; others go through a pinned staging buffer reused
+            // across loads.
+            const size_t bytes = sizeof(float) * 3 * n_points;
+            if (c->xyz_cap < 3 * n_points) {
                 CK(cudaStreamSynchronize(c->stream));
-                if (c->staging) cudaFreeHost(c->staging);
-                c->staging = nullptr;
-                c->staging_bytes = 0;
-                CK(cudaMallocHost(&c->staging, sizeof(float4) * n_points));
-                c->staging_bytes = sizeof(float4) * n_points;
-            } else {
-                CK(cudaStreamSynchronize(c->stream));  // the previous upload has left the staging buffer
+                dfree(c->xyz_dev);
+                c->xyz_dev = nullptr;
+                c->xyz_cap = 0;
+                CK(dalloc(&c->xyz_dev, (long long)(3 * n_points)));
+                c->xyz_cap = 3 * n_points;
             }
-            float4* tmp = (float4*)c->staging;
-            const float* f = (const float*)src;
-            for (size_t i = 0; i < n_points; ++i) tmp[i] = make_float4(f[3 * i], f[3 * i + 1], f[3 * i + 2], 1.0f);
-            CK(cudaMemcpyAsync(m.cp, tmp, sizeof(float4) * n_points, cudaMemcpyHostToDevice, c->stream));
+            cudaPointerAttributes attr{};
+            const bool pinned = cudaPointerGetAttributes(&attr, src) == cudaSuccess && attr.type == cudaMemoryTypeHost;
+            cudaGetLastError();  // a pageable pointer is not an error
+            const void* h = src;
+            if (!pinned) {
+                if (c->staging_bytes < bytes) {
+                    CK(cudaStreamSynchronize(c->stream));
+                    if (c->staging) cudaFreeHost(c->staging);
+                    c->staging = nullptr;
+                    c->staging_bytes = 0;
+                    CK(cudaMallocHost(&c->staging, bytes));
+                    c->staging_bytes = bytes;
+                } else {
+                    CK(cudaStreamSynchronize(c->stream));  // the previous upload has left the staging buffer
+                }
+                std::memcpy(c->staging, src, bytes);
+                h = c->staging;
+            }
+            CK(cudaMemcpyAsync(c->xyz_dev, h, bytes, cudaMemcpyHostToDevice, c->stream));
+            launch_widen_points(c->xyz_dev, m.cp, (long long)n_points, c->stream);
+            CK(cudaGetLastError());
+            // the caller's page-locked buffer is read asynchronously: done before returning
+            if (pinned && c->in_frame) CK(cudaStreamSynchronize(c->stream));
         }
         if (!c->in_frame) CK(cudaStreamSynchronize(c->stream));
     }

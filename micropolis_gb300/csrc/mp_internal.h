@@ -122,6 +122,8 @@ void launch_adjoint(const DrawDev* draws, const FrameDev& fr, const SubPatches& 
 
 // ---- microbenchmark (mp_raster.cu)
 void launch_image(const float4* color, const FrameDev& fr, unsigned char* rgb, cudaStream_t s);
+// (x, y, z) -> (x, y, z, 1) for n points (src/Reyes/PatchIndex.cpp:83-98)
+void launch_widen_points(const float* xyz, float4* out, long long n, cudaStream_t s);
 void launch_atomic_bench(unsigned long long* buf, long long n_slots, long long n_ops, int pattern, cudaStream_t s);
 
 }  // namespace mp

@@ -799,6 +799,11 @@ __global__ void image_kernel(const float4* __restrict__ color, FrameDev fr, unsi
 
 // 64-bit atomicMin throughput probe: pattern 0 = uniform random slots,
 // pattern 1 = each warp updates one 8x8-pixel tile (micropolygon-like locality).
+__global__ void widen_points_kernel(const float* __restrict__ xyz, float4* __restrict__ out, long long n) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        out[i] = make_float4(xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2], 1.0f);
+}
+
 __global__ void atomic_bench_kernel(unsigned long long* buf, long long n_slots, long long n_ops, int pattern) {
     long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     long long stride = (long long)gridDim.x * blockDim.x;
@@ -961,6 +966,10 @@ void launch_pass_resolve(const FrameDev& fr, const Framebuffer& fb, long long ba
 void launch_dice_debug(const DrawDev* draws, const FrameDev& fr, const SubPatches& sub, int count, float4* pos,
                        int2* pxl, float* depth, cudaStream_t s) {
     launch_dice_grid(draws, fr, sub, 0, count, pos, pxl, depth, s);
+}
+
+void launch_widen_points(const float* xyz, float4* out, long long n, cudaStream_t s) {
+    if (n > 0) widen_points_kernel<<<grid_for(n, 256), 256, 0, s>>>(xyz, out, n);
 }
 
 void launch_image(const float4* color, const FrameDev& fr, unsigned char* rgb, cudaStream_t s) {
