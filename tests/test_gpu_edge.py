@@ -234,3 +234,33 @@ def test_draw_views_equals_per_draw_calls(built, cuda):
     assert frames[0][0] == frames[1][0]
     for a, b in zip(frames[0][1], frames[1][1]):
         assert np.array_equal(a, b)
+
+
+def test_pinned_and_pageable_uploads_agree(built, cuda):
+    """mp_load_patches copies a page-locked source directly and a pageable one
+    through its staging buffer; both widen on the device to the same control
+    points, so the frames agree: depth exactly, colour except where two
+    micropolygons tie in depth (the emission order, and so which of them
+    wins, varies from run to run)."""
+    from micropolis_gb300 import scenes
+    from micropolis_gb300.renderer import Projection, renderer_for
+    torch = cuda
+    sc = scenes.mixed4096_1920x1080(n=256, width=640, height=360)
+    frames = []
+    for pinned in (False, True):
+        r = renderer_for(sc, "batched")
+        proj = Projection(sc.fovy, sc.near, (sc.width, sc.height))
+        for k, d in enumerate(sc.draws):
+            cp = np.ascontiguousarray(d.mesh.cp, np.float32)
+            if pinned:
+                cp = torch.from_numpy(cp).pin_memory().numpy()
+            r.load_patches(100 + k, cp, d.mesh.type)
+        r.prepare()
+        for k, d in enumerate(sc.draws):
+            r.draw_patches(100 + k, d.mv, proj, d.color)
+        r.finish()
+        frames.append(r.read_framebuffer())
+        r.close()
+    assert np.array_equal(frames[0][1], frames[1][1])
+    bad, _ = framebuffer_diff(frames[0][0], frames[0][1], frames[1][0], frames[1][1], REL_TOL)
+    assert bad <= COVERAGE_BUDGET * frames[0][1].size
