@@ -8,7 +8,9 @@ import pytest
 
 from micropolis_gb300 import _lib, mscene, scenes
 
-REF_SCENES = "/root/reference/testscene"
+# the reference's packed scenes, where its tree is present (the same
+# variable oracle/build_ref.sh reads)
+REF_SCENES = os.path.join(os.environ.get("MP_REFERENCE_DIR", "/root/reference"), "testscene")
 
 
 def _records():

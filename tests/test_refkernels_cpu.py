@@ -7,9 +7,9 @@ The reference's -cl-fast-relaxed-math build leaves the rounding of
 contractions, divisions, float-to-int conversions and native_sin open; the
 compiled kernels take the oracle's choices for the last three (the shim) and
 gcc's own contraction, which the oracle's R1 table follows.  So the diced
-grids agree bit for bit, and the frames meet the bar of the benchmark spec:
-depth and colour within 1e-5 relative per pixel except in fewer than 1e-4
-of the frame's pixels (tie pixels, where the two sides let a different one
+grids agree bit for bit, and the frames meet the framebuffer bar: depth
+and colour within 1e-5 relative per pixel except in fewer than 1e-4 of the
+frame's pixels (tie pixels, where the two sides let a different one
 of two equally deep micropolygons win).
 """
 import numpy as np
