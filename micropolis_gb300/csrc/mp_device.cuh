@@ -20,7 +20,7 @@
 //       R3 max(x, 0) ignores NaN (fmaxf)
 //       R4 float->int truncates and saturates, NaN -> 0 (cvt.rzi.s32.f32)
 //       R5 int arithmetic wraps modulo 2^32
-//       R6 native_sin = mp_sinf (Cody-Waite reduction, Taylor polynomials)
+//       R6 native_sin = mp_sinf (Cody-Waite reduction modulo pi, odd Taylor polynomial)
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -304,9 +304,9 @@ __device__ __forceinline__ float frcp(float y) { return __frcp_rn(y); }
 __device__ __forceinline__ float kdiv(float x, float y) { return fmul(x, frcp(y)); }
 
 
-// R6: sin/cos by Cody-Waite reduction with pi/2 = P1 + P2 + P3 (three floats
-// from the exact value of pi) and Taylor polynomials (degree 9 / 10) on
-// |r| <= pi/4, evaluated with fused multiply-adds.
+// Cosine for the adjoint's derivatives: Cody-Waite reduction with pi/2 =
+// P1 + P2 + P3 (three floats from the exact value of pi) and Taylor
+// polynomials (degree 9 / 10) on |r| <= pi/4, with fused multiply-adds.
 __device__ __forceinline__ void sincos_reduced(float x, float& sr, float& cr, int& q) {
     float k = rintf(fmul(x, 0x1.45f306p-1f));
     float r = ffma(-k, 0x1.921fb6p+0f, x);
@@ -325,13 +325,24 @@ __device__ __forceinline__ void sincos_reduced(float x, float& sr, float& cr, in
     pc = ffma(r2, pc, -0x1.0p-1f);
     cr = ffma(r2, pc, 1.0f);
 }
+// R6 native_sin: reduction by pi = PI1 + PI2 + PI3 (the pi/2 split doubled,
+// exactly) to |r| <= pi/2, the odd Taylor polynomial of degree 13, the sign
+// of (-1)^k; one polynomial instead of the two of sincos_reduced.
 __device__ __forceinline__ float mp_sinf(float x) {
     if (!isfinite(x)) return fsub(x, x);
-    float s, c;
-    int q;
-    sincos_reduced(x, s, c, q);
-    q &= 3;
-    return q == 0 ? s : q == 1 ? c : q == 2 ? -s : -c;
+    const float k = rintf(fmul(x, 0x1.45f306p-2f));
+    float r = ffma(-k, 0x1.921fb6p+1f, x);
+    r = ffma(-k, -0x1.777a5cp-24f, r);
+    r = ffma(-k, -0x1.ee59dap-49f, r);
+    const float r2 = fmul(r, r);
+    float p = ffma(r2, 0x1.612462p-33f, -0x1.ae6456p-26f);
+    p = ffma(r2, p, 0x1.71de3ap-19f);
+    p = ffma(r2, p, -0x1.a01a02p-13f);
+    p = ffma(r2, p, 0x1.111112p-7f);
+    p = ffma(r2, p, -0x1.555556p-3f);
+    const float sn = ffma(fmul(r, r2), p, r);
+    const float odd = fsub(k, fmul(2.0f, floorf(fmul(k, 0.5f))));
+    return odd != 0.0f ? -sn : sn;
 }
 __device__ __forceinline__ float mp_cosf(float x) {
     if (!isfinite(x)) return fsub(x, x);

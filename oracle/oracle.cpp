@@ -25,7 +25,8 @@
 //   R4  float -> int conversion truncates, saturates at the int range and
 //       maps NaN to 0 (the CUDA cvt.rzi.s32.f32 rule);
 //   R5  int arithmetic wraps modulo 2^32;
-//   R6  native_sin is or_sinf below (Cody-Waite reduction + Taylor series).
+//   R6  native_sin is or_sinf below (Cody-Waite reduction modulo pi + an odd
+//       Taylor polynomial).
 #include "oracle.h"
 
 #include <cmath>
@@ -303,9 +304,10 @@ static inline float kdiv(float x, float y) { return x * (1.0f / y); }
 
 }  // namespace
 
-// R6: sin/cos by Cody-Waite reduction with pi/2 = P1 + P2 + P3 (three floats
-// taken from the exact value of pi) and Taylor polynomials of degree 9 (sin)
-// and 10 (cos) on |r| <= pi/4, all in float with fused multiply-adds.
+// Cosine (the adjoint's derivative of the displacement) by Cody-Waite
+// reduction with pi/2 = P1 + P2 + P3 (three floats taken from the exact value
+// of pi) and Taylor polynomials of degree 9 (sin) and 10 (cos) on
+// |r| <= pi/4, all in float with fused multiply-adds.
 static const float kTwoOverPi = 0x1.45f306p-1f;
 static const float kP1 = 0x1.921fb6p+0f;
 static const float kP2 = -0x1.777a5cp-25f;
@@ -330,17 +332,29 @@ static inline void or_sincos_reduced(float x, float& sr, float& cr, int& q) {
     cr = std::fma(r2, pc, 1.0f);
 }
 
+// native_sin (R6): reduction by pi = PI1 + PI2 + PI3 (the pi/2 split above
+// doubled, exactly) to |r| <= pi/2, the odd Taylor polynomial of degree 13
+// in r, and the sign of (-1)^k.  Largest error 1.1e-7 absolute, 1.8 ulp.
+static const float kOneOverPi = 0x1.45f306p-2f;
+static const float kPi1 = 0x1.921fb6p+1f;
+static const float kPi2 = -0x1.777a5cp-24f;
+static const float kPi3 = -0x1.ee59dap-49f;
+
 extern "C" float or_sinf(float x) {
     if (!std::isfinite(x)) return x - x;
-    float s, c;
-    int q;
-    or_sincos_reduced(x, s, c, q);
-    switch (q & 3) {
-        case 0: return s;
-        case 1: return c;
-        case 2: return -s;
-        default: return -c;
-    }
+    const float k = std::rint(x * kOneOverPi);
+    float r = std::fma(-k, kPi1, x);
+    r = std::fma(-k, kPi2, r);
+    r = std::fma(-k, kPi3, r);
+    const float r2 = r * r;
+    float p = std::fma(r2, 0x1.612462p-33f, -0x1.ae6456p-26f);
+    p = std::fma(r2, p, 0x1.71de3ap-19f);
+    p = std::fma(r2, p, -0x1.a01a02p-13f);
+    p = std::fma(r2, p, 0x1.111112p-7f);
+    p = std::fma(r2, p, -0x1.555556p-3f);
+    const float sn = std::fma(r * r2, p, r);
+    const float odd = k - 2.0f * std::floor(k * 0.5f);
+    return odd != 0.0f ? -sn : sn;
 }
 
 extern "C" float or_cosf(float x) {
