@@ -102,7 +102,7 @@ __device__ __forceinline__ void bns_warp_loop(const DrawDev* draws, const int* _
                 break;
             }
             __nanosleep(sleep_ns);
-            if (sleep_ns < 2048) sleep_ns <<= 1;
+            if (sleep_ns < 512) sleep_ns <<= 1;
             continue;
         }
         idle = 0;
