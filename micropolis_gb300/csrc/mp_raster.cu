@@ -1,7 +1,8 @@
 // Dice, shade and rasterize kernels.
 //
-// Batched path: raster_fused dices each sub-patch into shared memory (one
-// warp per sub-patch, control points staged once per warp), applies the
+// Batched path: raster_fused dices groups of sub-patches into shared memory
+// (a block per group, the group's control points and matrices staged with
+// cp.async while the previous group is processed), applies the
 // reference's per-8x8-block rules (a block with a vertex at eye z == 0 is
 // dropped, kernels/reyes.cl:130-162; the block bound over front-facing quads
 // and its is_empty test of kernels/reyes.cl:287) and rasterizes every quad
