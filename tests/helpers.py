@@ -37,3 +37,36 @@ def golden_case(name):
     sc = scenes.Scene(name, int(z["width"]), int(z["height"]), [draw], fovy=float(z["fovy"]), near=float(z["near"]),
                       options=dict(opts))
     return sc, opts, z["pid"], z["range"]
+
+
+GOLDEN_FRAMES = ("frame_mixed96_bezier_512_d0_ps8", "frame_mixed96_bezier_512_d1_ps8",
+                 "frame_mixed96_gregory_512_d0_ps8", "frame_mixed96_gregory_depth3_512_d1_ps8",
+                 "frame_mixed96_bezier_512_d0_ps16")
+
+
+def golden_frame(name):
+    """(scene, options, colour float32[N,4], depth int32[N]) of a golden
+    framebuffer written by tests/golden/make_golden_frames.py from the
+    reference's own kernels; the options include the displacement and dice
+    grid it was rendered with."""
+    import os
+    z = np.load(os.path.join(GOLDEN_DIR, name + ".npz"))
+    sc, opts, _, _ = golden_case(str(z["case"]))
+    opts = dict(opts, displacement=int(z["displacement"]), reyes_patch_size=int(z["patch_size"]))
+    sc.options.update(opts)
+    n = int(z["pixels"])
+    color = np.empty((n, 4), np.float32)
+    color[:] = np.asarray(z["clear"], np.float32)
+    depth = np.full(n, 0x7fffffff, np.int32)
+    color[z["index"]] = z["color"]
+    depth[z["index"]] = z["depth"]
+    return sc, opts, color, depth
+
+
+def frame_agrees(color, depth, gcolor, gdepth, rel=1e-5, budget=1e-4):
+    """Coverage identical, and depth and colour within rel except in at most
+    budget of the frame's pixels (ties); returns the number of such pixels."""
+    assert np.array_equal(depth != 0x7fffffff, gdepth != 0x7fffffff)
+    bad, _ = framebuffer_diff(color, depth, gcolor, gdepth, rel)
+    assert bad <= budget * depth.size, (bad, depth.size)
+    return bad

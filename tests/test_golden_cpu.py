@@ -1,11 +1,12 @@
 """The oracle against golden vectors of the reference's own CPU
 bound-and-split (tests/golden/, written by tests/golden/make_golden.py from
 the reference's src/base/Patch.cpp and Projection.cpp): the same sub-patches,
-bit for bit, in the same emission order."""
+bit for bit, in the same emission order; and against golden framebuffers of
+the reference's own kernels (tests/golden/make_golden_frames.py)."""
 import numpy as np
 import pytest
 
-from helpers import GOLDEN_CASES, golden_case
+from helpers import GOLDEN_CASES, GOLDEN_FRAMES, frame_agrees, golden_case, golden_frame
 
 
 @pytest.mark.parametrize("name", GOLDEN_CASES)
@@ -16,3 +17,16 @@ def test_oracle_matches_golden(built, name):
     assert len(gpid) > 0
     assert np.array_equal(pid, gpid)
     assert np.array_equal(rng.view(np.uint32), grng.view(np.uint32))
+
+
+@pytest.mark.parametrize("name", GOLDEN_FRAMES)
+def test_oracle_matches_golden_frame(built, name):
+    """The oracle's frame against the reference kernels' own framebuffer
+    (tests/golden/make_golden_frames.py): identical coverage and clear
+    pixels, depth and colour within 1e-5 except in < 1e-4 of the pixels."""
+    from oracle import oracle
+    sc, opts, gcolor, gdepth = golden_frame(name)
+    col, dep, _ = oracle.render(sc, params=oracle.make_params(sc, **opts))
+    empty = gdepth == 0x7fffffff
+    assert np.array_equal(col[empty].view(np.uint32), gcolor[empty].view(np.uint32))
+    frame_agrees(col, dep, gcolor, gdepth)
