@@ -6,7 +6,10 @@ the LIFO loop of src/Reyes/BoundNSplitCLCPU.cpp:75-159 (oracle/ref_pin.cpp).
 Each fixture holds the inputs (control points, patch type, modelview,
 options) and the reference's emitted sub-patch sequence (patch id and range,
 in emission order), so the tests need neither the reference tree nor the
-scene generators.  Run here, where the reference tree exists:
+scene generators.  For three of the cases, gpucrit_<case>.npz holds the
+sub-patch set of the reference's GPU bound criterion on the same inputs:
+bound() of kernels/bound_n_split.h compiled as C++ (oracle/clshim/, driven
+by oracle/ref_kernels.cpp).  Run here, where the reference tree exists:
 
     python tests/golden/make_golden.py
 """
@@ -36,6 +39,15 @@ def cases():
     ]
 
 
+GPU_CRITERION_CASES = ("mixed96_bezier_512", "mixed96_gregory_512", "heightfield_eye_plane_512x384")
+
+
+def _one_draw(sc, k):
+    from micropolis_gb300 import scenes
+    return scenes.Scene(sc.name, sc.width, sc.height, [sc.draws[k]], fovy=sc.fovy, near=sc.near,
+                        options=dict(sc.options))
+
+
 def main():
     from oracle import oracle
     oracle.build_ref()
@@ -53,6 +65,13 @@ def main():
             cull_ribbon=np.float32(p.cull_ribbon), max_split_depth=np.int32(p.max_split_depth),
             pid=pid.astype(np.int32), range=rng.astype(np.float32))
         print(name, len(pid))
+        if name in GPU_CRITERION_CASES:
+            q = oracle.make_params(sc, bound_criterion=1, **over)
+            gsc = _one_draw(sc, k)
+            gpid, grng = oracle.ref_bound_n_split_gpu(gsc, 0, params=q)
+            np.savez_compressed(os.path.join(HERE, "gpucrit_" + name + ".npz"), pid=gpid.astype(np.int32),
+                                range=grng.astype(np.float32))
+            print("gpucrit_" + name, len(gpid))
 
 
 if __name__ == "__main__":

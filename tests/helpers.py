@@ -70,3 +70,14 @@ def frame_agrees(color, depth, gcolor, gdepth, rel=1e-5, budget=1e-4):
     bad, _ = framebuffer_diff(color, depth, gcolor, gdepth, rel)
     assert bad <= budget * depth.size, (bad, depth.size)
     return bad
+
+
+GOLDEN_GPU_CRITERION = ("mixed96_bezier_512", "mixed96_gregory_512", "heightfield_eye_plane_512x384")
+
+
+def golden_gpucrit(name):
+    """(pid, range) of the reference's GPU bound criterion on the inputs of
+    golden case `name` (tests/golden/make_golden.py): a set, in no order."""
+    import os
+    z = np.load(os.path.join(GOLDEN_DIR, "gpucrit_" + name + ".npz"))
+    return z["pid"], z["range"]

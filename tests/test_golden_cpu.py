@@ -6,7 +6,8 @@ the reference's own kernels (tests/golden/make_golden_frames.py)."""
 import numpy as np
 import pytest
 
-from helpers import GOLDEN_CASES, GOLDEN_FRAMES, frame_agrees, golden_case, golden_frame
+from helpers import (GOLDEN_CASES, GOLDEN_FRAMES, GOLDEN_GPU_CRITERION, frame_agrees, golden_case, golden_frame,
+                     golden_gpucrit, subpatch_set)
 
 
 @pytest.mark.parametrize("name", GOLDEN_CASES)
@@ -30,3 +31,15 @@ def test_oracle_matches_golden_frame(built, name):
     empty = gdepth == 0x7fffffff
     assert np.array_equal(col[empty].view(np.uint32), gcolor[empty].view(np.uint32))
     frame_agrees(col, dep, gcolor, gdepth)
+
+
+@pytest.mark.parametrize("name", GOLDEN_GPU_CRITERION)
+def test_oracle_gpu_criterion_matches_golden(built, name):
+    """The oracle's GPU bound criterion against the set of the reference's
+    own bound() (kernels/bound_n_split.h) on the same inputs."""
+    from oracle import oracle
+    sc, opts, _, _ = golden_case(name)
+    pid, rng, _ = oracle.bound_n_split(sc, params=oracle.make_params(sc, bound_criterion=1, **opts))
+    gpid, grng = golden_gpucrit(name)
+    assert len(gpid) > 0
+    assert subpatch_set(pid, rng) == subpatch_set(gpid, grng)

@@ -5,7 +5,8 @@ coverage, depth and colour within 1e-5 except in < 1e-4 of the pixels."""
 import numpy as np
 import pytest
 
-from helpers import GOLDEN_CASES, GOLDEN_FRAMES, frame_agrees, golden_case, golden_frame, subpatch_set
+from helpers import (GOLDEN_CASES, GOLDEN_FRAMES, GOLDEN_GPU_CRITERION, frame_agrees, golden_case, golden_frame,
+                     golden_gpucrit, subpatch_set)
 
 pytestmark = pytest.mark.gpu
 
@@ -35,4 +36,19 @@ def test_cuda_matches_golden_frame(built, cuda, name, path):
     # every pixel, the cleared ones included (the clear colour's powf runs on
     # this host, the fixture's where it was written)
     frame_agrees(col, dep, gcolor, gdepth)
+    r.close()
+
+
+@pytest.mark.parametrize("path", ["batched", "plain"])
+@pytest.mark.parametrize("name", GOLDEN_GPU_CRITERION)
+def test_cuda_gpu_criterion_matches_golden(built, cuda, name, path):
+    """With the GPU bound criterion, both paths emit the set of the
+    reference's own bound() on the same inputs, bit for bit."""
+    from micropolis_gb300.renderer import render_scene, renderer_for
+    sc, opts, _, _ = golden_case(name)
+    r = renderer_for(sc, path, bound_criterion=1, **opts)
+    render_scene(r, sc)
+    d, pid, rng = r.subpatches()
+    gpid, grng = golden_gpucrit(name)
+    assert subpatch_set(pid, rng, d) == subpatch_set(gpid, grng, np.zeros(len(gpid), np.int32))
     r.close()
