@@ -633,21 +633,45 @@ __device__ __forceinline__ unsigned long long key_of(const FrameDev& fr, const F
 
 // Colour of each pixel from its winning micropolygon: the diffuse factor the
 // fused kernel stored, the draw's colour (kernels/reyes.cl:191), and the
-// winning depth (kernels/reyes.cl:389).
+// winning depth (kernels/reyes.cl:389).  Each thread takes kResolvePixels
+// pixels a grid apart and issues their key loads, then their gathers, before
+// any use, so the dependent loads of several pixels are in flight at once.
+constexpr int kResolvePixels = 4;
 template <int PS>
 __global__ void resolve_kernel(const DrawDev* __restrict__ draws, FrameDev fr, SubPatches sub, Framebuffer fb,
                                const float* __restrict__ mshade) {
-    long long n = fb.pixels * fb.views;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        const unsigned long long key = key_of(fr, fb, i);
-        if (key == kClearKey) {
-            fb.color[i] = make_float4(fr.clear[0], fr.clear[1], fr.clear[2], fr.clear[3]);
-            fb.depth[i] = 0x7fffffff;
-        } else {
-            const unsigned id = (unsigned)(key & 0xffffffffu);
-            const int draw = sub.meta[id / (PS * PS)].y;
-            fb.color[i] = shade_color(mshade[id], draws[draw].color);
-            fb.depth[i] = (int)(key >> 32);
+    const long long n = fb.pixels * fb.views;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i0 = (long long)blockIdx.x * blockDim.x + threadIdx.x; i0 < n; i0 += kResolvePixels * stride) {
+        unsigned long long key[kResolvePixels];
+#pragma unroll
+        for (int u = 0; u < kResolvePixels; ++u) {
+            const long long i = i0 + u * stride;
+            key[u] = i < n ? key_of(fr, fb, i) : kClearKey;
+        }
+        int draw[kResolvePixels];
+        float m[kResolvePixels];
+#pragma unroll
+        for (int u = 0; u < kResolvePixels; ++u) {
+            draw[u] = 0;
+            m[u] = 0.0f;
+            if (key[u] != kClearKey) {
+                const unsigned id = (unsigned)(key[u] & 0xffffffffu);
+                draw[u] = sub.meta[id / (PS * PS)].y;
+                m[u] = mshade[id];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < kResolvePixels; ++u) {
+            const long long i = i0 + u * stride;
+            if (i >= n) break;
+            if (key[u] == kClearKey) {
+                fb.color[i] = make_float4(fr.clear[0], fr.clear[1], fr.clear[2], fr.clear[3]);
+                fb.depth[i] = 0x7fffffff;
+            } else {
+                fb.color[i] = shade_color(m[u], draws[draw[u]].color);
+                fb.depth[i] = (int)(key[u] >> 32);
+            }
         }
     }
 }
@@ -916,7 +940,7 @@ void launch_raster_big(const DrawDev*, const FrameDev& fr, const Framebuffer& fb
 
 void launch_resolve(const DrawDev* draws, const FrameDev& fr, const SubPatches& sub, const Framebuffer& fb,
                     const float* mshade, cudaStream_t s) {
-    int g = grid_for(fb.pixels * fb.views, 256);
+    int g = grid_for((fb.pixels * fb.views + kResolvePixels - 1) / kResolvePixels, 256);
     if (fr.PS == 16)
         resolve_kernel<16><<<g, 256, 0, s>>>(draws, fr, sub, fb, mshade);
     else
