@@ -615,7 +615,10 @@ __global__ void clear_kernel(Framebuffer fb, FrameDev fr, int with_color) {
     const long long nk = fb.key_pixels * fb.views, n = fb.pixels * fb.views;
     const float4 cc = make_float4(fr.clear[0], fr.clear[1], fr.clear[2], fr.clear[3]);
     const long long stride = (long long)gridDim.x * blockDim.x;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nk; i += stride) fb.keys[i] = kClearKey;
+    // the key buffer is a whole number of 32x32 tiles per view: two keys per 16-byte store
+    ulonglong2* k2 = reinterpret_cast<ulonglong2*>(fb.keys);
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nk / 2; i += stride)
+        k2[i] = make_ulonglong2(kClearKey, kClearKey);
     if (with_color)
         for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
             fb.color[i] = cc;
@@ -890,7 +893,11 @@ int grid_for(long long n, int block) {
 // launchers
 
 void launch_clear(const Framebuffer& fb, const FrameDev& fr, int with_color, cudaStream_t s) {
-    clear_kernel<<<grid_for(fb.key_pixels * fb.views, 256), 256, 0, s>>>(fb, fr, with_color);
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const long long want = with_color ? fb.pixels * fb.views : fb.key_pixels * fb.views / 2;
+    clear_kernel<<<(int)std::min<long long>(grid_for(want, 256), (long long)sms * 8), 256, 0, s>>>(fb, fr, with_color);
 }
 
 int raster_fused_grid(int PS, int group) {
