@@ -24,20 +24,6 @@ namespace mp {
 
 namespace {
 
-__global__ void bns_reset_kernel(unsigned long long* ctrl, long long roots) {
-    *cw(ctrl, kQTail) = ((unsigned long long)roots << 32) | (unsigned long long)roots;
-    *cw(ctrl, kQHead) = 0;
-    *cw(ctrl, kOutstanding) = 0;
-    *cw(ctrl, kOutCount) = 0;
-    *cw(ctrl, kDone) = roots == 0 ? 1 : 0;
-    *cw(ctrl, kStatus) = 0;
-    *cw(ctrl, kEpoch) = *cw(ctrl, kEpoch) + 1;
-    *cw(ctrl, kRoots) = (unsigned long long)roots;
-    *cw(ctrl, kBigCount) = 0;
-    *cw(ctrl, kFragments) = 0;
-    *cw(ctrl, kBigOverflow) = 0;
-    *cw(ctrl, kGroupTicket) = 0;
-}
 
 constexpr int kBnsBlock = 128;
 constexpr int kBnsSmemDraws = 64;
@@ -251,9 +237,6 @@ __global__ void reset_scan_kernel(unsigned long long* state, long long n_tiles, 
 // ---------------------------------------------------------------------------
 // launchers
 
-void launch_bns_reset(unsigned long long* ctrl, long long roots, cudaStream_t s) {
-    bns_reset_kernel<<<1, 1, 0, s>>>(ctrl, roots);
-}
 
 int bns_persistent_grid(int criterion) {
     int dev = 0, sms = 0, per_sm = 0;

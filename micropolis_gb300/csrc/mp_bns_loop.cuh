@@ -37,6 +37,23 @@ __device__ __forceinline__ unsigned lanemask_lt() {
     return m;
 }
 
+// The per-frame reset of the bound-and-split control words: roots tickets
+// filled and outstanding, counters cleared, the frame epoch advanced.
+__device__ __forceinline__ void bns_reset(unsigned long long* ctrl, long long roots) {
+    *cw(ctrl, kQTail) = ((unsigned long long)roots << 32) | (unsigned long long)roots;
+    *cw(ctrl, kQHead) = 0;
+    *cw(ctrl, kOutstanding) = 0;
+    *cw(ctrl, kOutCount) = 0;
+    *cw(ctrl, kDone) = roots == 0 ? 1 : 0;
+    *cw(ctrl, kStatus) = 0;
+    *cw(ctrl, kEpoch) = *cw(ctrl, kEpoch) + 1;
+    *cw(ctrl, kRoots) = (unsigned long long)roots;
+    *cw(ctrl, kBigCount) = 0;
+    *cw(ctrl, kFragments) = 0;
+    *cw(ctrl, kBigOverflow) = 0;
+    *cw(ctrl, kGroupTicket) = 0;
+}
+
 __device__ __forceinline__ void set_status(unsigned long long* ctrl, int code) {
     atomicCAS(cw(ctrl, kStatus), 0ull, (unsigned long long)code);
 }

@@ -434,8 +434,7 @@ mp_status capture_frame(mp_ctx* c, int n, long long roots) {
     cudaMemcpyAsync(c->d_draws, c->h_draws, sizeof(DrawDev) * (size_t)n, cudaMemcpyHostToDevice, c->stream);
     cudaMemcpyAsync(c->d_root_prefix, c->h_root_prefix, sizeof(int) * (size_t)(n + 1), cudaMemcpyHostToDevice,
                     c->stream);
-    launch_bns_reset(c->ctrl, roots, c->stream);
-    launch_clear(c->fb, c->fr, 0, c->stream);
+    launch_clear(c->fb, c->fr, 0, c->stream, c->ctrl, roots);
     launch_middle(c, n);
     launch_raster_big(c->d_draws, c->fr, c->fb, c->big, c->big_cap, c->ctrl, c->stream);
     launch_resolve(c->d_draws, c->fr, c->sub, c->fb, c->mshade, c->stream);
@@ -482,8 +481,7 @@ mp_status batched_frame(mp_ctx* c) {
             CK(cudaMemcpyAsync(c->d_root_prefix, c->h_root_prefix, sizeof(int) * (size_t)(n + 1),
                                cudaMemcpyHostToDevice, c->stream));
             CK(cudaEventRecord(c->ev0, c->stream));
-            launch_bns_reset(c->ctrl, roots, c->stream);
-            launch_clear(c->fb, c->fr, 0, c->stream);
+            launch_clear(c->fb, c->fr, 0, c->stream, c->ctrl, roots);
             CK(cudaEventRecord(c->sev[0], c->stream));
             if (overlapped(c)) {
                 // one launch: reported under dice+raster, bound&split shows 0
@@ -899,9 +897,8 @@ mp_status mp_prepare(mp_ctx* c) {
     for (double& v : c->stats.stage_ms) v = 0;
     if (c->opt.path == MP_PATH_PLAIN) {
         CK(cudaEventRecord(c->ev0, c->stream));
-        launch_bns_reset(c->ctrl, 0, c->stream);
-        launch_clear(c->fb, c->fr, 1, c->stream);
-        c->plain_kernels += 2;
+        launch_clear(c->fb, c->fr, 1, c->stream, c->ctrl, 0);
+        c->plain_kernels += 1;
         CK(cudaGetLastError());
     }
     return MP_OK;
@@ -953,7 +950,7 @@ mp_status mp_finish(mp_ctx* c) {
         c->stats.bounds = (long long)(hc(c, kQTail) >> 32);
         c->stats.passes = 1;
         // reset, clear, (bound-and-split, dice+raster | one overlapped kernel), exact slow raster, resolve
-        c->stats.kernels = overlapped(c) ? 5 : 6;
+        c->stats.kernels = overlapped(c) ? 4 : 5;
     } else {
         CK(cudaEventRecord(c->ev1, c->stream));
         st = read_ctrl(c);

@@ -69,7 +69,6 @@ struct Framebuffer {
 enum { kOk = 0, kErrInvalidArg = 1, kErrOutOfMemory = 2, kErrOverflow = 3, kErrTimeout = 4, kErrCuda = 5 };
 
 // ---- bound-and-split (mp_bns.cu)
-void launch_bns_reset(unsigned long long* ctrl, long long roots, cudaStream_t s);
 void launch_bns_persistent(const DrawDev* draws, const int* root_prefix, int n_draws, const FrameDev& fr,
                            const Queue& q, const SubPatches& out, unsigned long long* ctrl, int grid,
                            long long spin_limit, cudaStream_t s);
@@ -85,7 +84,10 @@ void launch_inclusive_scan_i32(const int* in, int* out, long long n, unsigned lo
 long long scan_state_words(long long n);
 
 // ---- dice / shade / raster / resolve (mp_raster.cu)
-void launch_clear(const Framebuffer& fb, const FrameDev& fr, int with_color, cudaStream_t s);
+// clears the key buffer (and with_color: colour and depth); with reset_ctrl,
+// also resets the frame's bound-and-split control words for `roots` roots
+void launch_clear(const Framebuffer& fb, const FrameDev& fr, int with_color, cudaStream_t s,
+                  unsigned long long* reset_ctrl = nullptr, long long roots = 0);
 void launch_raster_fused(const DrawDev* draws, const FrameDev& fr, const SubPatches& sub, const Framebuffer& fb,
                          float* mshade, BigQuad* big, long long big_cap, unsigned long long* ctrl, int grid, int group,
                          cudaStream_t s);

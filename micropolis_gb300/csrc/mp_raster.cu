@@ -611,7 +611,10 @@ __global__ void __launch_bounds__(kBigThreads) raster_big_kernel(FrameDev fr, Fr
     if (blockIdx.x == 0 && threadIdx.x == 0 && n > 0) atomicAdd(cw(ctrl, kBigTotal), (unsigned long long)n);
 }
 
-__global__ void clear_kernel(Framebuffer fb, FrameDev fr, int with_color) {
+__global__ void clear_kernel(Framebuffer fb, FrameDev fr, int with_color, unsigned long long* reset_ctrl,
+                             long long roots) {
+    // the frame's bound-and-split reset rides along (one thread)
+    if (reset_ctrl && blockIdx.x == 0 && threadIdx.x == 0) bns_reset(reset_ctrl, roots);
     const long long nk = fb.key_pixels * fb.views, n = fb.pixels * fb.views;
     const float4 cc = make_float4(fr.clear[0], fr.clear[1], fr.clear[2], fr.clear[3]);
     const long long stride = (long long)gridDim.x * blockDim.x;
@@ -892,12 +895,14 @@ int grid_for(long long n, int block) {
 // ---------------------------------------------------------------------------
 // launchers
 
-void launch_clear(const Framebuffer& fb, const FrameDev& fr, int with_color, cudaStream_t s) {
+void launch_clear(const Framebuffer& fb, const FrameDev& fr, int with_color, cudaStream_t s,
+                  unsigned long long* reset_ctrl, long long roots) {
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const long long want = with_color ? fb.pixels * fb.views : fb.key_pixels * fb.views / 2;
-    clear_kernel<<<(int)std::min<long long>(grid_for(want, 256), (long long)sms * 8), 256, 0, s>>>(fb, fr, with_color);
+    clear_kernel<<<(int)std::min<long long>(grid_for(want, 256), (long long)sms * 8), 256, 0, s>>>(fb, fr, with_color,
+                                                                                             reset_ctrl, roots);
 }
 
 int raster_fused_grid(int PS, int group) {

@@ -43,7 +43,7 @@ def test_knobs_match_oracle(built, cuda, ps, groups):
                 d, p, g = r.subpatches()
                 assert subpatch_set(p, g, d) == want, (tile, group, overlap)
                 assert r.stats()["fragments"] == ost["fragments"], (tile, group, overlap)
-                assert r.stats()["kernels"] == (5 if overlap else 6)
+                assert r.stats()["kernels"] == (4 if overlap else 5)
                 col, dep = r.read_framebuffer()
                 bad, _ = framebuffer_diff(col, dep, ocol, odep, REL_TOL)
                 assert bad <= COVERAGE_BUDGET * dep.size, (tile, group, overlap, bad)
