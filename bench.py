@@ -90,6 +90,13 @@ class ClockSampler:
                 stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except (FileNotFoundError, OSError):
             self.proc = None
+        # nvidia-smi's start-up (driver queries) delays CUDA calls made while it
+        # runs: wait for its first sample before the timed region starts
+        t0 = time.perf_counter()
+        while self.proc and time.perf_counter() - t0 < 5.0 and self.proc.poll() is None:
+            if os.path.exists(self.path) and os.path.getsize(self.path) > 0:
+                break
+            time.sleep(0.01)
         return self
 
     def __exit__(self, *exc):

@@ -79,8 +79,12 @@ typedef struct {
     int64_t subpatch_capacity;      /* emitted sub-patches per frame */
     int64_t spin_limit;             /* bounded-wait iterations before MP_ERR_TIMEOUT */
     /* batched path: run bound&split and rasterization in one launch that
-     * rasterizes sub-patches while they are being emitted (1) or as two
-     * launches (0); bns_blocks = blocks that start with bound&split (0 = auto) */
+     * rasterizes sub-patches while they are being emitted (1) or as separate
+     * launches (0, the default).  With 1 the sub-patches keep the order in
+     * which they were emitted, which depends on scheduling, so the winner
+     * between two equally deep micropolygons can differ between runs; with 0
+     * they are put in the canonical order first (see mp_subpatches).
+     * bns_blocks = blocks that start with bound&split (0 = auto) */
     int32_t overlap;
     int32_t bns_blocks;
     /* tuning knobs that do not change the image (0 = default):
@@ -109,10 +113,11 @@ typedef struct {
     int64_t fragments;              /* covered (micropolygon, pixel) pairs */
     int64_t big_quads;              /* quads on the exact slow raster path */
     double gpu_ms;                  /* device time of the last frame (CUDA events) */
-    /* per-stage device times of the last frame when stage timing is on
-     * (mp_set_stage_timing); stages: 0 clear+reset, 1 bound&split, 2 dice+raster
-     * (plain: dice), 3 exact slow raster, 4 resolve (plain: shade), 5 plain sample,
-     * 6 plain pass resolve, 7 plain host readback gaps */
+    /* per-stage device times of the last frame (batched path: always, from
+     * events inside its graph; plain path: with stage timing on,
+     * mp_set_stage_timing); stages: 0 clear+reset, 1 bound&split, 2 dice+raster
+     * (plain: dice), 3 exact slow raster, 4 resolve (plain: shade), 5 canonical
+     * order sort (plain: sample), 6 plain pass resolve, 7 plain host readback gaps */
     double stage_ms[8];
     int64_t kernels;                /* kernel launches of the last frame (graph nodes included) */
 } mp_stats;
@@ -173,10 +178,13 @@ mp_status mp_finish(mp_ctx* ctx);
 mp_status mp_set_stage_timing(mp_ctx* ctx, int32_t on);
 /* Renderer::dump_trace (Renderer.h:43): the last frame's device commands as
  * `name@queue:queued:submit:start:end:id:deps` lines (src/CL/Device.cpp:275-289),
- * times in ns from the start of the frame, deps '|'-separated ids.  With stage
- * timing on (mp_set_stage_timing) one line per stage (per pass on the plain
- * path), else one line for the frame.  NUL-terminated; MP_ERR_OVERFLOW when
- * the text did not fit in cap bytes (buf then holds the lines that fit). */
+ * times in ns from the start of the frame, deps '|'-separated ids, named with
+ * the reference's command names (those its tools/trace_summary.py maps).
+ * Batched path: one line per stage.  Plain path: one line per command of each
+ * pass, with stage timing on (mp_set_stage_timing); without it the plain path
+ * records no times and the call returns MP_ERR_STATE.  NUL-terminated;
+ * MP_ERR_OVERFLOW when the text did not fit in cap bytes (buf then holds the
+ * lines that fit). */
 mp_status mp_dump_trace(mp_ctx* ctx, char* buf, size_t cap);
 
 /* Headless framebuffer (replaces OGLSharedFramebuffer, src/Reyes/Framebuffer.cpp:75-144):
@@ -194,7 +202,15 @@ mp_status mp_copy_framebuffer_device(mp_ctx* ctx, int32_t view, void* color_dev,
  * sub-patch index * reyes_patch_size^2 + nu + nv * reyes_patch_size, or -1. */
 mp_status mp_read_visibility(mp_ctx* ctx, int32_t view, int64_t* ids);
 /* Sub-patches of the last frame, for parity checks: count, then up to cap records
- * (draw index, patch id, range min.x min.y max.x max.y).  Any pointer may be NULL. */
+ * (draw index, patch id, range min.x min.y max.x max.y).  Any pointer may be NULL.
+ * Record s owns the micropolygon numbers s * reyes_patch_size^2 + nu + nv *
+ * reyes_patch_size (mp_read_visibility).  On the batched path the records
+ * are in the canonical order: ascending root (the draw's first patch, counted
+ * over the frame's draws in call order, + patch id), then split path (the
+ * patch's split tree depth first, low half before high half), the same on
+ * every run; the reference's CPU bound-and-split emits the same set in its
+ * stack order (src/Reyes/BoundNSplitCLCPU.cpp:75-159).  On the plain path they
+ * are in pass order. */
 mp_status mp_subpatches(mp_ctx* ctx, int64_t* count, int32_t* draw, int32_t* pid, float* range, int64_t cap);
 mp_status mp_stats_get(mp_ctx* ctx, mp_stats* stats);
 
@@ -212,6 +228,11 @@ mp_status mp_backward(mp_ctx* ctx, int32_t view, const void* grad_color_dev, voi
 /* Sets the displacement amplitude multiplier (the 0.04/0.02/0.01 amplitudes of
  * kernels/dice.cl:52-54 are scaled by it) for the following frames. */
 mp_status mp_set_displacement_amplitude(mp_ctx* ctx, float amplitude);
+/* Same, from one float in device memory, copied on the context's stream
+ * (no host synchronization): the differentiable path's amplitude stays on
+ * the device.  The reference fixes the amplitudes in the dice kernel
+ * (kernels/dice.cl:52-54); the multiplier is this core's parameter. */
+mp_status mp_set_displacement_amplitude_device(mp_ctx* ctx, const void* amp_dev);
 /* Replaces the control points of a loaded handle in place from device memory (same count). */
 mp_status mp_update_patches_device(mp_ctx* ctx, uint64_t handle, const void* dev_xyz1);
 
@@ -229,7 +250,9 @@ mp_status mp_inclusive_scan(mp_ctx* ctx, const int32_t* host_in, int32_t* host_o
  * first call on a device looks up that array's device address, so make it
  * before any stream capture.  All calls on a device share the array: calls
  * that overlap on the GPU race and must be serialized by the caller.  Runs on
- * `stream` (a cudaStream_t, NULL = default stream) and returns when done. */
+ * `stream` (a cudaStream_t, NULL = default stream) and returns when the scan
+ * is done: it synchronizes `stream` and reads the scan's status word back to
+ * the host (MP_ERR_TIMEOUT when a bounded wait gave up). */
 mp_status mp_inclusive_scan_noalloc(const int32_t* in_dev, int32_t* out_dev, int64_t n, void* stream);
 
 /* The image the reference shows for one layer (shaders/tex_draw.frag: gamma

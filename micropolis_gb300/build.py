@@ -16,7 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libmpcore.so")
-SOURCES = ["mp_bns.cu", "mp_raster.cu", "mp_adjoint.cu", "mp_host.cu", "mp_noalloc.cu", "mp_scene.cu"]
+SOURCES = ["mp_bns.cu", "mp_sort.cu", "mp_raster.cu", "mp_adjoint.cu", "mp_host.cu", "mp_noalloc.cu", "mp_scene.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-prec-div=true", "-prec-sqrt=true", "-ftz=false",
          "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off", "--expt-relaxed-constexpr"]

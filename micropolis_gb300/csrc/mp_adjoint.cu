@@ -86,10 +86,12 @@ __device__ __forceinline__ void vertex_forward(const DrawDev& d, const FrameDev&
 
 constexpr int kAdjBlock = 256;
 
-__global__ void __launch_bounds__(kAdjBlock) adjoint_kernel(const DrawDev* __restrict__ draws, FrameDev fr,
+__global__ void __launch_bounds__(kAdjBlock) adjoint_kernel(const DrawDev* __restrict__ draws, FrameDev frp,
                                                             SubPatches sub, Framebuffer fb,
                                                             const float4* __restrict__ grad_color, float* grad_amp,
                                                             int view) {
+    FrameDev fr = frp;
+    load_amplitude(fr);
     const int PS = fr.PS;
     const int lane = threadIdx.x & 31;
     long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;

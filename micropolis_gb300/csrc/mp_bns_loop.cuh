@@ -52,6 +52,7 @@ __device__ __forceinline__ void bns_reset(unsigned long long* ctrl, long long ro
     *cw(ctrl, kFragments) = 0;
     *cw(ctrl, kBigOverflow) = 0;
     *cw(ctrl, kGroupTicket) = 0;
+    *cw(ctrl, kMaxDepth) = 0;
 }
 
 __device__ __forceinline__ void set_status(unsigned long long* ctrl, int code) {
@@ -88,6 +89,7 @@ __device__ __forceinline__ void bns_warp_loop(const DrawDev* draws, const int* _
     unsigned long long ticket = kNoTicket;
     long long idle = 0;
     unsigned sleep_ns = 32;
+    unsigned max_depth = 0;   // deepest emitted sub-patch of this warp so far (lane 0)
     while (true) {
         // hand new tickets to the lanes that have none
         unsigned need = __ballot_sync(0xffffffffu, ticket == kNoTicket);
@@ -126,6 +128,7 @@ __device__ __forceinline__ void bns_warp_loop(const DrawDev* draws, const int* _
         sleep_ns = 32;
         float4 r = make_float4(0.f, 0.f, 1.f, 1.f);
         int pid = 0, draw = 0, depth = 0;
+        unsigned path = 0;
         int dec = -1;
         if (ready) {
             int flag = kInheritNone;
@@ -145,6 +148,7 @@ __device__ __forceinline__ void bns_warp_loop(const DrawDev* draws, const int* _
                 pid = (int)m.x;
                 draw = (int)(m.y & 0xffffffu);
                 depth = (int)(m.y >> 24);
+                if (q.path) path = __ldcg(q.path + slot);
                 if (inherit) flag = load_inherited(q.pts + slot * kPtsPerSlot, sp, st);
             }
             if (inherit)
@@ -161,9 +165,15 @@ __device__ __forceinline__ void bns_warp_loop(const DrawDev* draws, const int* _
         const unsigned smask = __ballot_sync(0xffffffffu, split);
         const long long n_child = 2ll * __popc(smask);
         const long long net = n_child - (long long)__popc(rmask);
+        const unsigned emit_depth = __reduce_max_sync(0xffffffffu, dec == kDraw ? (unsigned)depth : 0u);
         unsigned long long obase = 0, old = 0, tbase = 0;
         if (lane == 0) {
             if (emask) obase = atomicAdd(cw(ctrl, kOutCount), (unsigned long long)__popc(emask));
+            if (emit_depth > max_depth) {
+                // the sort packs the frame's keys into root bits above this many path bits
+                max_depth = emit_depth;
+                atomicMax(cw(ctrl, kMaxDepth), (unsigned long long)emit_depth);
+            }
             old = atomicAdd(cw(ctrl, kQTail), ((unsigned long long)n_child << 32) + (unsigned long long)net);
             tbase = atomicAdd(cw(ctrl, kQHead), (unsigned long long)__popc(rmask));
         }
@@ -176,6 +186,7 @@ __device__ __forceinline__ void bns_warp_loop(const DrawDev* draws, const int* _
             if ((long long)o < out.capacity) {
                 out.range[o] = r;
                 out.meta[o] = make_int2(pid, draw);
+                if (out.path) out.path[o] = path;
                 // consumers running in the same launch wait for this flag
                 if (out_seq) st_release_u32(out_seq + o, epoch);
             } else {
@@ -195,6 +206,11 @@ __device__ __forceinline__ void bns_warp_loop(const DrawDev* draws, const int* _
                 q.range[s0 + 1] = c1;
                 q.meta[s0] = make_uint2((unsigned)pid, meta_y);
                 q.meta[s0 + 1] = make_uint2((unsigned)pid, meta_y);
+                if (q.path) {
+                    // the high half sets bit 31 - depth (paths deeper than 32 keep their first 32 bits)
+                    q.path[s0] = path;
+                    q.path[s0 + 1] = depth < 32 ? path | (0x80000000u >> depth) : path;
+                }
                 if (inherit) {
                     store_inherited(q.pts + s0 * kPtsPerSlot, dec, 0, depth + 1, sp, st);
                     store_inherited(q.pts + (s0 + 1) * kPtsPerSlot, dec, 1, depth + 1, sp, st);

@@ -60,7 +60,8 @@ struct FrameDev {
     int max_depth;         // max_split_depth
     int backface;          // backface_culling
     int displacement;      // displacement on/off
-    float fdisp[3];        // 0.04, 0.02, 0.01 times the amplitude multiplier
+    float fdisp[3];        // 0.04, 0.02, 0.01 times the amplitude multiplier (load_amplitude)
+    const float* amp_dev;  // the amplitude multiplier in device memory (nullptr: fdisp as given)
     float clear[4];        // clear colour (powf(c, 2.2), alpha 1000)
     int gx, gy;            // 8-pixel tile grid of the output framebuffer
     int n_draws;
@@ -429,6 +430,19 @@ __device__ __forceinline__ float4 mul_m44v4(const float* m, float4 v) {
     r01 = ffma2(make_float2(m[12], m[13]), w, r01);
     r23 = ffma2(make_float2(m[14], m[15]), w, r23);
     return make_float4(r01.x, r01.y, r23.x, r23.y);
+}
+
+// The displacement amplitudes of a frame: kernels/dice.cl:52-54's 0.04,
+// 0.02 and 0.01 times the multiplier held in device memory, so that a caller
+// can change it between frames from device data.  Kernels that displace call
+// this once on their copy of the frame constants.
+__device__ __forceinline__ void load_amplitude(FrameDev& fr) {
+    if (fr.amp_dev && fr.displacement) {
+        const float a = *(volatile const float*)fr.amp_dev;
+        fr.fdisp[0] = fmul(0.04f, a);
+        fr.fdisp[1] = fmul(0.02f, a);
+        fr.fdisp[2] = fmul(0.01f, a);
+    }
 }
 
 // kernels/dice.cl:51-67 -- eye-space displacement, updated coordinates used

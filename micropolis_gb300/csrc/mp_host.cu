@@ -62,7 +62,10 @@ struct mp_ctx {
     int* h_root_prefix = nullptr;
     int draws_cap = 0;
     Queue q{};
-    SubPatches sub{};
+    SubPatches sub{};                 // bound-and-split output, in emission order
+    SubPatches sorted{};              // the same in canonical order (batched path, two launches)
+    SortBuffers sb{};
+    int sort_passes = 0;              // radix passes captured for this frame
     BigQuad* big = nullptr;
     long long big_cap = 0;
     float* mshade = nullptr;          // diffuse factor per micropolygon (batched path)
@@ -87,7 +90,7 @@ struct mp_ctx {
     cudaGraphExec_t graph = nullptr;
     int graph_draws = -1;
     long long graph_roots = -1;
-    const void* graph_key[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    const void* graph_key[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     // set by every reallocation of a buffer the graph's kernels use: a new
     // allocation may land at the freed one's address, so the pointers above
     // cannot tell that the captured sizes and pointers are stale
@@ -112,6 +115,7 @@ struct mp_ctx {
     std::vector<TraceEvent> trace;
     unsigned char* image = nullptr;   // device buffer of mp_read_image
     long long image_bytes = 0;
+    float* d_amp = nullptr;           // displacement amplitude multiplier read by the displacing kernels
 };
 
 namespace {
@@ -161,6 +165,20 @@ void perspective(float fovy_rad, float aspect, float zn, float zf, float* m) {
 long long auto_queue_cap(long long roots) { return std::min(std::max(1LL << 22, roots * 32), 1LL << 28); }
 long long auto_sub_cap(long long roots) { return std::min(std::max(1LL << 21, roots * 64), 1LL << 26); }
 
+void free_sorted(mp_ctx* c) {
+    dfree(c->sorted.range);
+    dfree(c->sorted.meta);
+    c->sorted = SubPatches{};
+    for (int k = 0; k < 2; ++k) {
+        dfree(c->sb.keys[k]);
+        dfree(c->sb.vals[k]);
+    }
+    dfree(c->sb.hist);
+    dfree(c->sb.counts);
+    dfree(c->sb.group_counts);
+    c->sb = SortBuffers{};
+}
+
 mp_status grow_queue(mp_ctx* c, long long need) {
     if (need <= c->q.capacity) return MP_OK;
     c->graph_stale = true;
@@ -169,11 +187,13 @@ mp_status grow_queue(mp_ctx* c, long long need) {
     cudaFree(c->q.meta);
     cudaFree(c->q.seq);
     cudaFree(c->q.pts);
+    cudaFree(c->q.path);
     c->q = Queue{};
     CK(dalloc(&c->q.range, cap));
     CK(dalloc(&c->q.meta, cap));
     CK(dalloc(&c->q.seq, cap));
     CK(dalloc(&c->q.pts, cap * kPtsPerSlot));
+    CK(dalloc(&c->q.path, cap));
     CK(cudaMemsetAsync(c->q.seq, 0, sizeof(unsigned) * (size_t)cap, c->stream));
     c->q.capacity = cap;
     return MP_OK;
@@ -189,6 +209,7 @@ mp_status grow_sub(mp_ctx* c, long long need, bool keep) {
     CK(dalloc(&n.range, cap));
     CK(dalloc(&n.meta, cap));
     CK(dalloc(&n.seq, cap));
+    CK(dalloc(&n.path, cap));
     CK(cudaMemsetAsync(n.seq, 0, sizeof(unsigned) * (size_t)cap, c->stream));
     n.capacity = cap;
     if (keep && c->sub.capacity > 0) {
@@ -201,7 +222,28 @@ mp_status grow_sub(mp_ctx* c, long long need, bool keep) {
     cudaFree(c->sub.range);
     cudaFree(c->sub.meta);
     cudaFree(c->sub.seq);
+    cudaFree(c->sub.path);
     c->sub = n;
+    // the canonical list and the sort's scratch follow the emitted list's capacity
+    free_sorted(c);
+    SubPatches o{};
+    CK(dalloc(&o.range, cap));
+    CK(dalloc(&o.meta, cap));
+    o.capacity = cap;
+    c->sorted = o;
+    SortBuffers b{};
+    b.capacity = cap;
+    b.tiles = sort_tiles(cap);
+    b.groups = (b.tiles + kSortGroup - 1) / kSortGroup;
+    c->sb = b;
+    for (int k = 0; k < 2; ++k) {
+        CK(dalloc(&c->sb.keys[k], cap));
+        CK(dalloc(&c->sb.vals[k], cap));
+    }
+    CK(dalloc(&c->sb.hist, 2 * kSortPasses * 256));
+    CK(dalloc(&c->sb.counts, c->sb.tiles * 256));
+    CK(dalloc(&c->sb.group_counts, kSortPasses * c->sb.groups * 256));
+    CK(cudaMemsetAsync(c->sb.hist, 0, sizeof(unsigned) * 2 * kSortPasses * 256, c->stream));
     return MP_OK;
 }
 
@@ -414,32 +456,105 @@ int bns_blocks(const mp_ctx* c) {
     return std::max(1, c->frame_grid / 3);
 }
 
-// bound-and-split and rasterization: one overlapped launch or two launches
-void launch_middle(mp_ctx* c, int n) {
+// The sub-patch list the frame's micropolygon ids index: the canonical list
+// on the batched path in separate launches, else the list as emitted.
+const SubPatches& final_list(const mp_ctx* c) {
+    return c->opt.path == MP_PATH_BATCHED && !overlapped(c) ? c->sorted : c->sub;
+}
+
+// Kernel launches of one batched frame.
+long long batched_kernels(const mp_ctx* c) {
+    // clear+reset, (bound-and-split, sort keys, sort passes, dice+raster | overlapped), slow raster, resolve
+    if (overlapped(c)) return 4;
+    return 5 + 1 + c->sort_passes;
+}
+
+void launch_sort(mp_ctx* c) {
+    launch_canonical_sort(c->d_root_prefix, c->sub, c->sorted, c->sb, c->ctrl, c->opt.spin_limit, c->sort_passes,
+                          c->stream);
+}
+
+// Stages of a batched frame in launch order: the mp_stats.stage_ms slot
+// and the trace name of each.  Names are the reference's command names,
+// which its tools/trace_summary.py maps: bound-and-split is "bound & split";
+// the canonical-order sort, a radix sort built on prefix sums, takes the
+// name of the reference's prefix-sum command, "accumulate" (both count as
+// subdivision there); the fused dice+shade+raster launch is "dice", the
+// exact slow raster "sample", the colour resolve "shade".
+struct StageMark {
+    int slot;
+    const char* name;
+};
+constexpr int kBatchedStages = 6;
+constexpr StageMark kStageMarks[kBatchedStages] = {{0, "clear framebuffer"}, {1, "bound & split"}, {5, "accumulate"},
+                                                   {2, "dice"},              {3, "sample"},        {4, "shade"}};
+
+// Event sev[k] marks the end of stage k - 1 (sev[0] the start).  Inside a
+// stream capture the record becomes an event node of the graph.
+void mark(mp_ctx* c, int k, bool capturing) {
+    if (capturing)
+        cudaEventRecordWithFlags(c->sev[k], c->stream, cudaEventRecordExternal);
+    else
+        cudaEventRecord(c->sev[k], c->stream);
+}
+
+// The device work of one batched frame, from the upload of the draw
+// constants to the read-back of the control words, with an event after each
+// stage: bound-and-split, canonical order and rasterization as separate
+// launches, or (option `overlap`) bound-and-split and rasterization as one
+// overlapped launch over the list in emission order.
+void enqueue_frame(mp_ctx* c, int n, long long roots, bool capturing) {
+    cudaMemcpyAsync(c->d_draws, c->h_draws, sizeof(DrawDev) * (size_t)n, cudaMemcpyHostToDevice, c->stream);
+    cudaMemcpyAsync(c->d_root_prefix, c->h_root_prefix, sizeof(int) * (size_t)(n + 1), cudaMemcpyHostToDevice,
+                    c->stream);
+    mark(c, 0, capturing);
+    launch_clear(c->fb, c->fr, 0, c->stream, c->ctrl, roots);
+    mark(c, 1, capturing);
     if (overlapped(c)) {
+        // one launch, reported as dice+raster; bound-and-split and sort show 0
+        mark(c, 2, capturing);
+        mark(c, 3, capturing);
         launch_frame_kernel(c->d_draws, c->d_root_prefix, n, c->fr, c->q, c->sub, c->fb, c->mshade, c->big, c->big_cap,
                             c->ctrl, c->opt.spin_limit, c->frame_grid, bns_blocks(c), c->opt.dice_group, c->stream);
     } else {
         launch_bns_persistent(c->d_draws, c->d_root_prefix, n, c->fr, c->q, c->sub, c->ctrl, c->bns_grid,
                               c->opt.spin_limit, c->stream);
-        launch_raster_fused(c->d_draws, c->fr, c->sub, c->fb, c->mshade, c->big, c->big_cap, c->ctrl, c->raster_grid,
-                            c->opt.dice_group, c->stream);
+        mark(c, 2, capturing);
+        launch_sort(c);
+        mark(c, 3, capturing);
+        launch_raster_fused(c->d_draws, c->fr, c->sorted, c->fb, c->mshade, c->big, c->big_cap, c->ctrl,
+                            c->raster_grid, c->opt.dice_group, c->stream);
     }
+    mark(c, 4, capturing);
+    launch_raster_big(c->d_draws, c->fr, c->fb, c->big, c->big_cap, c->ctrl, c->stream);
+    mark(c, 5, capturing);
+    launch_resolve(c->d_draws, c->fr, final_list(c), c->fb, c->mshade, c->stream);
+    mark(c, 6, capturing);
+    cudaMemcpyAsync(c->h_ctrl, c->ctrl, sizeof(unsigned long long) * kNumCtrl * kCtrlStride, cudaMemcpyDeviceToHost,
+                    c->stream);
+}
+
+// Stage times and trace lines of the last batched frame (its events have completed).
+void read_stage_events(mp_ctx* c) {
+    c->trace.clear();
+    for (double& v : c->stats.stage_ms) v = 0;
+    float t = 0;
+    for (int k = 0; k < kBatchedStages; ++k) {
+        float ms = 0;
+        if (cudaEventElapsedTime(&ms, c->sev[k], c->sev[k + 1]) != cudaSuccess) ms = 0;
+        c->stats.stage_ms[kStageMarks[k].slot] = ms;
+        if (!(overlapped(c) && (k == 1 || k == 2)))
+            c->trace.push_back({kStageMarks[k].name, (long long)(t * 1e6), (long long)((t + ms) * 1e6)});
+        t += ms;
+    }
+    cudaGetLastError();
 }
 
 mp_status capture_frame(mp_ctx* c, int n, long long roots) {
     invalidate_graph(c);
     cudaGraph_t g = nullptr;
     CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-    cudaMemcpyAsync(c->d_draws, c->h_draws, sizeof(DrawDev) * (size_t)n, cudaMemcpyHostToDevice, c->stream);
-    cudaMemcpyAsync(c->d_root_prefix, c->h_root_prefix, sizeof(int) * (size_t)(n + 1), cudaMemcpyHostToDevice,
-                    c->stream);
-    launch_clear(c->fb, c->fr, 0, c->stream, c->ctrl, roots);
-    launch_middle(c, n);
-    launch_raster_big(c->d_draws, c->fr, c->fb, c->big, c->big_cap, c->ctrl, c->stream);
-    launch_resolve(c->d_draws, c->fr, c->sub, c->fb, c->mshade, c->stream);
-    cudaMemcpyAsync(c->h_ctrl, c->ctrl, sizeof(unsigned long long) * kNumCtrl * kCtrlStride, cudaMemcpyDeviceToHost,
-                    c->stream);
+    enqueue_frame(c, n, roots, true);
     cudaError_t e = cudaStreamEndCapture(c->stream, &g);
     if (e != cudaSuccess) return cuda_fail(c, e, "cudaStreamEndCapture");
     e = cudaGraphInstantiate(&c->graph, g, 0);
@@ -453,6 +568,7 @@ mp_status capture_frame(mp_ctx* c, int n, long long roots) {
     c->graph_key[2] = c->big;
     c->graph_key[3] = c->d_draws;
     c->graph_key[4] = c->mshade;
+    c->graph_key[5] = c->sorted.range;
     return MP_OK;
 }
 
@@ -474,62 +590,32 @@ mp_status batched_frame(mp_ctx* c) {
     if ((st = grow_queue(c, qcap)) || (st = grow_sub(c, scap, false)) || (st = grow_big(c, 1 << 16)) ||
         (st = ensure_mshade(c)))
         return st;
+    const int passes = canonical_sort_passes(c->opt.max_split_depth, roots);
+    if (passes != c->sort_passes) {
+        c->sort_passes = passes;
+        c->graph_stale = true;
+    }
     for (int attempt = 0; attempt < 8; ++attempt) {
         if (c->stage_timing) {
-            // the same launches as the graph, with an event after each stage
-            CK(cudaMemcpyAsync(c->d_draws, c->h_draws, sizeof(DrawDev) * (size_t)n, cudaMemcpyHostToDevice, c->stream));
-            CK(cudaMemcpyAsync(c->d_root_prefix, c->h_root_prefix, sizeof(int) * (size_t)(n + 1),
-                               cudaMemcpyHostToDevice, c->stream));
+            // the graph's launches issued one by one (same events)
             CK(cudaEventRecord(c->ev0, c->stream));
-            launch_clear(c->fb, c->fr, 0, c->stream, c->ctrl, roots);
-            CK(cudaEventRecord(c->sev[0], c->stream));
-            if (overlapped(c)) {
-                // one launch: reported under dice+raster, bound&split shows 0
-                CK(cudaEventRecord(c->sev[1], c->stream));
-                launch_middle(c, n);
-            } else {
-                launch_bns_persistent(c->d_draws, c->d_root_prefix, n, c->fr, c->q, c->sub, c->ctrl, c->bns_grid,
-                                      c->opt.spin_limit, c->stream);
-                CK(cudaEventRecord(c->sev[1], c->stream));
-                launch_raster_fused(c->d_draws, c->fr, c->sub, c->fb, c->mshade, c->big, c->big_cap, c->ctrl,
-                                    c->raster_grid, c->opt.dice_group, c->stream);
-            }
-            CK(cudaEventRecord(c->sev[2], c->stream));
-            launch_raster_big(c->d_draws, c->fr, c->fb, c->big, c->big_cap, c->ctrl, c->stream);
-            CK(cudaEventRecord(c->sev[3], c->stream));
-            launch_resolve(c->d_draws, c->fr, c->sub, c->fb, c->mshade, c->stream);
-            CK(cudaEventRecord(c->sev[4], c->stream));
+            enqueue_frame(c, n, roots, false);
             CK(cudaEventRecord(c->ev1, c->stream));
-            CK(cudaMemcpyAsync(c->h_ctrl, c->ctrl, sizeof(unsigned long long) * kNumCtrl * kCtrlStride,
-                               cudaMemcpyDeviceToHost, c->stream));
             CK(cudaStreamSynchronize(c->stream));
             CK(cudaGetLastError());
-            float ms = 0, t = 0;
-            cudaEvent_t prev = c->ev0;
-            // command names of the reference's trace (tools/trace_summary.py maps these): the fused
-            // dice+shade+raster launch is reported as dice, the exact slow raster as sample and
-            // the colour resolve as shade
-            static const char* const names[5] = {"clear framebuffer", "bound & split", "dice", "sample", "shade"};
-            c->trace.clear();
-            for (int k = 0; k < 5; ++k) {
-                cudaEventElapsedTime(&ms, prev, c->sev[k]);
-                c->stats.stage_ms[k] = ms;
-                c->trace.push_back({names[k], (long long)(t * 1e6), (long long)((t + ms) * 1e6)});
-                t += ms;
-                prev = c->sev[k];
-            }
         } else {
-        if (!c->graph || c->graph_stale || c->graph_draws != n || c->graph_roots != roots ||
-            c->graph_key[0] != c->q.range || c->graph_key[1] != c->sub.range || c->graph_key[2] != c->big ||
-            c->graph_key[3] != c->d_draws || c->graph_key[4] != c->mshade) {
-            st = capture_frame(c, n, roots);
-            if (st) return st;
+            if (!c->graph || c->graph_stale || c->graph_draws != n || c->graph_roots != roots ||
+                c->graph_key[0] != c->q.range || c->graph_key[1] != c->sub.range || c->graph_key[2] != c->big ||
+                c->graph_key[3] != c->d_draws || c->graph_key[4] != c->mshade || c->graph_key[5] != c->sorted.range) {
+                st = capture_frame(c, n, roots);
+                if (st) return st;
+            }
+            CK(cudaEventRecord(c->ev0, c->stream));
+            CK(cudaGraphLaunch(c->graph, c->stream));
+            CK(cudaEventRecord(c->ev1, c->stream));
+            CK(cudaStreamSynchronize(c->stream));
         }
-        CK(cudaEventRecord(c->ev0, c->stream));
-        CK(cudaGraphLaunch(c->graph, c->stream));
-        CK(cudaEventRecord(c->ev1, c->stream));
-        CK(cudaStreamSynchronize(c->stream));
-        }
+        read_stage_events(c);
         unsigned long long status = hc(c, kStatus);
         if (status != kErrOverflow) {
             if (status) return check_status(c, status);
@@ -689,6 +775,10 @@ mp_status mp_create(const mp_options* opts, mp_ctx** out) {
         if (err != cudaSuccess && st == MP_OK) st = cuda_fail(c, err, w);
     };
     ck(dalloc(&c->ctrl, (long long)kNumCtrl * kCtrlStride), "ctrl");
+    ck(dalloc(&c->d_amp, 1), "amplitude");
+    ck(cudaMemcpyAsync(c->d_amp, &o.displacement_amplitude, sizeof(float), cudaMemcpyHostToDevice, c->stream),
+       "amplitude");
+    fr.amp_dev = c->d_amp;
     ck(cudaMemsetAsync(c->ctrl, 0, sizeof(unsigned long long) * kNumCtrl * kCtrlStride, c->stream), "ctrl memset");
     ck(cudaMallocHost((void**)&c->h_ctrl, sizeof(unsigned long long) * kNumCtrl * kCtrlStride), "h_ctrl");
     c->fb.pixels = (long long)W * H;
@@ -727,6 +817,7 @@ void mp_destroy(mp_ctx* c) {
     invalidate_graph(c);
     for (auto& kv : c->meshes) dfree(kv.second.cp);
     dfree(c->ctrl);
+    dfree(c->d_amp);
     if (c->h_ctrl) cudaFreeHost(c->h_ctrl);
     if (c->staging) cudaFreeHost(c->staging);
     dfree(c->xyz_dev);
@@ -734,8 +825,9 @@ void mp_destroy(mp_ctx* c) {
     dfree(c->d_root_prefix);
     if (c->h_draws) cudaFreeHost(c->h_draws);
     if (c->h_root_prefix) cudaFreeHost(c->h_root_prefix);
-    dfree(c->q.range); dfree(c->q.meta); dfree(c->q.seq); dfree(c->q.pts);
-    dfree(c->sub.range); dfree(c->sub.meta); dfree(c->sub.seq);
+    dfree(c->q.range); dfree(c->q.meta); dfree(c->q.seq); dfree(c->q.pts); dfree(c->q.path);
+    dfree(c->sub.range); dfree(c->sub.meta); dfree(c->sub.seq); dfree(c->sub.path);
+    free_sorted(c);
     dfree(c->big);
     dfree(c->mshade);
     dfree(c->fb.keys); dfree(c->fb.color); dfree(c->fb.depth);
@@ -858,7 +950,16 @@ mp_status mp_set_displacement_amplitude(mp_ctx* c, float amp) {
     c->fr.fdisp[0] = 0.04f * amp;
     c->fr.fdisp[1] = 0.02f * amp;
     c->fr.fdisp[2] = 0.01f * amp;
-    invalidate_graph(c);  // the frame constants are kernel parameters of the graph
+    // the kernels read the multiplier from device memory: a stream-ordered
+    // write, no new graph (a pageable source is staged before the call returns)
+    CK(cudaMemcpyAsync(c->d_amp, &amp, sizeof(float), cudaMemcpyHostToDevice, c->stream));
+    return MP_OK;
+}
+
+mp_status mp_set_displacement_amplitude_device(mp_ctx* c, const void* amp_dev) {
+    if (!c || !amp_dev) return MP_ERR_INVALID_ARG;
+    if (c->in_frame) return fail(c, MP_ERR_STATE, "amplitude change inside a frame");
+    CK(cudaMemcpyAsync(c->d_amp, amp_dev, sizeof(float), cudaMemcpyDeviceToDevice, c->stream));
     return MP_OK;
 }
 
@@ -949,8 +1050,7 @@ mp_status mp_finish(mp_ctx* c) {
         c->stats.subpatches = std::min((long long)hc(c, kOutCount), c->sub.capacity);
         c->stats.bounds = (long long)(hc(c, kQTail) >> 32);
         c->stats.passes = 1;
-        // reset, clear, (bound-and-split, dice+raster | one overlapped kernel), exact slow raster, resolve
-        c->stats.kernels = overlapped(c) ? 4 : 5;
+        c->stats.kernels = batched_kernels(c);
     } else {
         CK(cudaEventRecord(c->ev1, c->stream));
         st = read_ctrl(c);
@@ -1004,11 +1104,10 @@ mp_status mp_dump_trace(mp_ctx* c, char* buf, size_t cap) {
     buf[0] = 0;
     size_t pos = 0;
     const char* queue = c->opt.path == MP_PATH_PLAIN ? "plain" : "batched";
-    if (c->trace.empty()) {
-        const long long end_ns = (long long)(c->stats.gpu_ms * 1e6);
-        if (!put(buf, cap, &pos, "frame@%s:0:0:0:%lld:0:\n", queue, end_ns)) return MP_ERR_OVERFLOW;
-        return MP_OK;
-    }
+    if (!c->frame_valid) return fail(c, MP_ERR_STATE, "no finished frame");
+    if (c->trace.empty())
+        return fail(c, MP_ERR_STATE,
+                    "the plain path times its commands only with stage timing on (mp_set_stage_timing)");
     for (size_t i = 0; i < c->trace.size(); ++i) {
         const auto& e = c->trace[i];
         // each command depends on the one before it on the stream
@@ -1035,8 +1134,11 @@ mp_status mp_dump_stats(mp_ctx* c, char* buf, size_t cap) {
     } mem[] = {
         {"control points", cp},
         {"work queue", c->q.capacity * (long long)(sizeof(float4) * (1 + kPtsPerSlot) + sizeof(uint2) +
-                                                   sizeof(unsigned))},
-        {"sub-patch list", c->sub.capacity * (long long)(sizeof(float4) + sizeof(int2) + sizeof(unsigned))},
+                                                   2 * sizeof(unsigned))},
+        {"sub-patch list", c->sub.capacity * (long long)(sizeof(float4) + sizeof(int2) + 2 * sizeof(unsigned))},
+        {"canonical sub-patch list", c->sorted.capacity * (long long)(sizeof(float4) + sizeof(int2))},
+        {"canonical order sort", c->sb.capacity * 2 * (long long)(sizeof(unsigned long long) + sizeof(unsigned)) +
+                                     (c->sb.tiles + kSortPasses * c->sb.groups) * 256 * (long long)sizeof(unsigned)},
         {"diffuse factors", c->mshade_cap * (long long)sizeof(float)},
         {"framebuffer", c->fb.key_pixels * c->fb.views * 8 + c->fb.pixels * c->fb.views * 20},
         {"exact slow raster quads", c->big_cap * (long long)sizeof(BigQuad)},
@@ -1149,8 +1251,9 @@ mp_status mp_subpatches(mp_ctx* c, int64_t* count, int32_t* draw, int32_t* pid, 
     if (k <= 0) return MP_OK;
     std::vector<float4> r((size_t)k);
     std::vector<int2> m((size_t)k);
-    CK(cudaMemcpyAsync(r.data(), c->sub.range, sizeof(float4) * (size_t)k, cudaMemcpyDeviceToHost, c->stream));
-    CK(cudaMemcpyAsync(m.data(), c->sub.meta, sizeof(int2) * (size_t)k, cudaMemcpyDeviceToHost, c->stream));
+    const SubPatches& list = final_list(c);
+    CK(cudaMemcpyAsync(r.data(), list.range, sizeof(float4) * (size_t)k, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(m.data(), list.meta, sizeof(int2) * (size_t)k, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     for (long long i = 0; i < k; ++i) {
         if (draw) draw[i] = m[(size_t)i].y;
@@ -1233,7 +1336,7 @@ mp_status mp_backward(mp_ctx* c, int32_t view, const void* grad_color_dev, void*
         c->h_draws[i].grad_cp = (size_t)i < c->grad_ptr.size() ? c->grad_ptr[(size_t)i] : nullptr;
     }
     CK(cudaMemcpyAsync(c->d_draws, c->h_draws, sizeof(DrawDev) * (size_t)n, cudaMemcpyHostToDevice, c->stream));
-    launch_adjoint(c->d_draws, c->fr, c->sub, c->fb, (const float4*)grad_color_dev, (float*)grad_amp_dev, view,
+    launch_adjoint(c->d_draws, c->fr, final_list(c), c->fb, (const float4*)grad_color_dev, (float*)grad_amp_dev, view,
                    c->stream);
     CK(cudaGetLastError());
     return MP_OK;

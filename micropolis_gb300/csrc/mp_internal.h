@@ -27,7 +27,9 @@ enum CtrlWord {
     kBigOverflow,      // big quads that did not fit
     kBigTotal,         // big quads rasterized over the frame
     kGroupTicket,      // sub-patch groups claimed by the frame kernel's rasterizers
-    kNumCtrl
+    kMaxDepth,         // deepest split path of an emitted sub-patch (canonical sort keys)
+    kSortTicket,       // tile tickets of the canonical sort, one word per radix pass (kSortPasses)
+    kNumCtrl = kSortTicket + 8
 };
 constexpr int kCtrlStride = 16;  // unsigned long long words per line
 
@@ -38,6 +40,9 @@ struct Queue {              // bound-and-split work queue (structure of arrays)
     // kPtsPerSlot float4 per slot: six of the item's nine bound samples, taken
     // from its parent, and which three are missing (or nullptr: none kept)
     float4* pts;
+    // split path of each range: bit 31 - d is 1 when the range is the high
+    // half of its depth-d ancestor's split (nullptr: not kept)
+    unsigned* path;
     long long capacity;
 };
 
@@ -46,7 +51,24 @@ struct SubPatches {         // emitted sub-patch list
     int2* meta;             // (patch id, draw)
     long long capacity;
     unsigned* seq;          // epoch of the frame that emitted the slot (frame kernel only)
+    unsigned* path;         // split path (Queue::path) of each sub-patch (nullptr: not kept)
 };
+
+// Canonical order of a frame's sub-patches: ascending (root, split path),
+// root = the draw's first root + patch id.  Scratch of the radix sort that
+// establishes it (mp_sort.cu).
+constexpr int kSortPasses = 8;          // 8-bit digits of the 64-bit key
+struct SortBuffers {
+    unsigned long long* keys[2];        // ping-pong keys
+    unsigned* vals[2];                  // ping-pong source slots
+    unsigned* hist;                     // 2 (frame parity) x kSortPasses x 256 digit counts
+    unsigned* counts;                   // per pass: digit counts of each tile, tiles x 256
+    unsigned* group_counts;             // kSortPasses x groups x 256: counts of groups of kSortGroup tiles
+    long long capacity;                 // keys per buffer
+    long long tiles;                    // tiles at capacity
+    long long groups;                   // tile groups at capacity
+};
+constexpr int kSortGroup = 16;          // tiles per group of the pass's prefix
 
 struct BigQuad {            // a quad rasterized by the exact tile emulation
     int px[4], py[4];
@@ -82,6 +104,18 @@ void launch_bns_pass(const DrawDev* draws, const FrameDev& fr, const Queue& stac
 void launch_inclusive_scan_i32(const int* in, int* out, long long n, unsigned long long* scan_state,
                                unsigned long long* ctrl, long long spin_limit, cudaStream_t s);
 long long scan_state_words(long long n);
+
+// ---- canonical sub-patch order (mp_sort.cu)
+long long sort_tiles(long long n);
+// Sorts the n_out (device count kOutCount) sub-patches of `in` by (root,
+// path) and gathers them into `out`; root_prefix as for bound-and-split.
+// Launches the radix passes of digits [0, n_passes) (a pass whose digit is
+// the same for every key of the frame returns at once).
+void launch_canonical_sort(const int* root_prefix, const SubPatches& in, const SubPatches& out, const SortBuffers& sb,
+                           unsigned long long* ctrl, long long spin_limit, int n_passes, cudaStream_t s);
+// The radix passes the keys of a frame can need: root bits up to `roots`
+// above at most min(32, max_split_depth + 1) path bits.
+int canonical_sort_passes(int max_split_depth, long long roots);
 
 // ---- dice / shade / raster / resolve (mp_raster.cu)
 // clears the key buffer (and with_color: colour and depth); with reset_ctrl,

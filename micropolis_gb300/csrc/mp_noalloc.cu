@@ -176,9 +176,16 @@ extern "C" mp_status mp_inclusive_scan_noalloc(const int32_t* in_dev, int32_t* o
     }
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     const int tiles = (int)((n + kNoAllocTileItems - 1) / kNoAllocTileItems);
+    // an error left by the caller's earlier work stays the caller's: only a
+    // launch error of this call (which replaces it) is reported, and cleared
+    const cudaError_t before = cudaPeekAtLastError();
     noalloc_reset_kernel<<<1, 256, 0, s>>>(scratch, tiles);
     noalloc_scan_kernel<<<tiles, kNoAllocBlock, 0, s>>>(in_dev, out_dev, n, scratch);
-    if (cudaGetLastError() != cudaSuccess) return MP_ERR_CUDA;
+    const cudaError_t after = cudaPeekAtLastError();
+    if (after != cudaSuccess && after != before) {
+        cudaGetLastError();
+        return MP_ERR_CUDA;
+    }
     unsigned long long status = 0;
     if (cudaMemcpyAsync(&status, scratch + kWordStatus, sizeof(status), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
         cudaStreamSynchronize(s) != cudaSuccess) {

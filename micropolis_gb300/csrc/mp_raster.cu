@@ -122,8 +122,9 @@ __device__ __forceinline__ int raster_quad_fast(const FrameDev& fr, unsigned lon
             bool in1 = tri_test(t1, tx, ty, depth);
             bool in2 = tri_test(t2, tx, ty, depth);
             if (in1 || in2) {
-                unsigned long long key = ((unsigned long long)idepth_of(depth) << 32) | mp_id;
-                atomicMin(keys + key_index(fr, x, y), key);
+                // the reference writes only depths below the cleared 0x7fffffff (kernels/reyes.cl:389)
+                const unsigned idp = idepth_of(depth);
+                if (idp < 0x7fffffffu) atomicMin(keys + key_index(fr, x, y), ((unsigned long long)idp << 32) | mp_id);
                 ++frags;
             }
         }
@@ -430,11 +431,16 @@ __device__ __forceinline__ void raster_group(FusedSmem<PS, NS>& sm, int b, long 
 
 template <int PS, int NS>
 __global__ void __launch_bounds__(fused_threads<NS>(), 768 / fused_threads<NS>())
-    raster_fused_kernel(const DrawDev* __restrict__ draws, FrameDev fr, SubPatches sub, Framebuffer fb,
+    raster_fused_kernel(const DrawDev* __restrict__ draws, FrameDev frp, SubPatches sub, Framebuffer fb,
                         float* __restrict__ mshade, BigQuad* big, long long big_cap, unsigned long long* ctrl) {
     using SM = FusedSmem<PS, NS>;
+    FrameDev fr = frp;
+    load_amplitude(fr);
     extern __shared__ __align__(16) unsigned char smem_raw[];
     SM& sm = *reinterpret_cast<SM*>(smem_raw);
+    // an earlier stage of the frame failed (the host reports it): the list
+    // may be incomplete, so nothing is rasterized
+    if (*(volatile unsigned long long*)cw(ctrl, kStatus) != 0) return;
     long long S = (long long)*(volatile unsigned long long*)cw(ctrl, kOutCount);
     if (S > sub.capacity) S = sub.capacity;
     const V3 light = light_dir();
@@ -473,10 +479,12 @@ constexpr size_t frame_smem() {
 
 template <int PS, int NS>
 __global__ void __launch_bounds__(fused_threads<NS>(), 768 / fused_threads<NS>())
-    frame_kernel(const DrawDev* __restrict__ gdraws, const int* __restrict__ root_prefix, int n_draws, FrameDev fr,
+    frame_kernel(const DrawDev* __restrict__ gdraws, const int* __restrict__ root_prefix, int n_draws, FrameDev frp,
                  Queue q, SubPatches sub, Framebuffer fb, float* __restrict__ mshade, BigQuad* big, long long big_cap,
                  unsigned long long* ctrl, long long spin_limit, int n_bns_ctas) {
     using SM = FusedSmem<PS, NS>;
+    FrameDev fr = frp;
+    load_amplitude(fr);
     // bound-and-split blocks: draw records, then the bound samples of each thread
     // (frame_smem() sizes the launch for both uses)
     constexpr int kStaged = kFrameStagedDraws;
@@ -598,8 +606,9 @@ __global__ void __launch_bounds__(kBigThreads) raster_big_kernel(FrameDev fr, Fr
             bool in1 = tri_test(t1, tx, ty, depth);
             bool in2 = tri_test(t2, tx, ty, depth);
             if (in1 || in2) {
-                unsigned long long key = ((unsigned long long)idepth_of(depth) << 32) | b.mp_id;
-                atomicMin(keys + key_index(fr, x, y), key);
+                const unsigned idp = idepth_of(depth);
+                if (idp < 0x7fffffffu)
+                    atomicMin(keys + key_index(fr, x, y), ((unsigned long long)idp << 32) | b.mp_id);
                 ++frags;
             }
         }
@@ -686,8 +695,10 @@ __global__ void resolve_kernel(const DrawDev* __restrict__ draws, FrameDev fr, S
 // Plain per-pass kernels
 
 template <int PS>
-__global__ void dice_grid_kernel(const DrawDev* __restrict__ draws, FrameDev fr, SubPatches sub, long long base,
+__global__ void dice_grid_kernel(const DrawDev* __restrict__ draws, FrameDev frp, SubPatches sub, long long base,
                                  int count, float4* pos_grid, int2* pxl_grid, float* depth_grid) {
+    FrameDev fr = frp;
+    load_amplitude(fr);
     constexpr int G = PS + 1, NV = G * G;
     long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= (long long)count * NV) return;

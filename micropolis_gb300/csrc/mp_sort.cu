@@ -1,0 +1,381 @@
+// Canonical order of a frame's emitted sub-patches.
+//
+// Bound-and-split emits sub-patches in whatever order its warps finish
+// them, and the rasterizer numbers micropolygons by their sub-patch's list
+// position (ties in depth go to the smaller number).  So that a frame's
+// numbering, its winners at depth ties and everything read back from it are
+// the same on every run, the list is put into one canonical order before
+// rasterization: ascending (root, split path), where root = the draw's first
+// root + patch id (draws in call order, as the reference's Scene::draw
+// issues them, src/micropolis/Scene.cpp:179-197) and the split path holds,
+// from the root down, 1 for each split whose high half the sub-patch lies in
+// (bit 31 - d for the split at depth d).  Within one patch that is the
+// depth-first order of its split tree, low half first.  The oracle numbers
+// its sub-patches in the same order, so the two break ties identically.
+//
+// The sort is a least-significant-digit radix sort over 8-bit digits of a
+// key that packs the root above the frame's D path bits (D = the deepest
+// emitted sub-patch, which bound-and-split records; below bit 32 - D every
+// path is zero, so the order is that of (root << 32 | path)).  Digit counts
+// of every pass are taken once, up front (Adinets & Merrill's one-sweep
+// radix sort).  A pass splits the keys into tiles, one per resident block
+// at a time (rounds of gridDim.x tiles): each tile ranks its digits stably
+// (per-warp counters; lanes with equal digits found by one ballot per digit
+// bit), publishes its digit counts, waits until every tile of its round and
+// the earlier ones has published, adds up the counts of the tiles before it
+// (independent loads, no chain of waits), and scatters.  The last pass that
+// moves keys writes the sub-patch records themselves in canonical order.
+//   keys  -- keys, identity source slots, digit counts of every pass;
+//   pass  -- one launch per digit position the frame's keys can have; a pass
+//            whose digit is the same for every key returns at once.
+// Every wait is bounded (MP_ERR_TIMEOUT, no scatter after it).
+#include "mp_bns_loop.cuh"
+
+namespace mp {
+
+namespace {
+
+constexpr int kKeysBlock = 1024;
+constexpr int kSortBlock = 512;
+constexpr int kSortWarps = kSortBlock / 32;
+constexpr int kSortItems = 16;
+constexpr int kSortTile = kSortBlock * kSortItems;   // keys per tile
+constexpr int kDigits = 256;
+
+__device__ __forceinline__ long long sort_count(const unsigned long long* ctrl, const SubPatches& in,
+                                                const SortBuffers& sb) {
+    long long n = (long long)*(volatile const unsigned long long*)(ctrl + kOutCount * kCtrlStride);
+    if (n > in.capacity) n = in.capacity;
+    if (n > sb.capacity) n = sb.capacity;
+    return n;
+}
+
+__device__ __forceinline__ unsigned frame_epoch(const unsigned long long* ctrl) {
+    return (unsigned)*(volatile const unsigned long long*)(ctrl + kEpoch * kCtrlStride);
+}
+
+// Counts of the frame's passes: one table per frame parity, so that a
+// frame clears the next frame's table while its own is read.
+__device__ __forceinline__ unsigned* hist_of(const SortBuffers& sb, unsigned epoch) {
+    return sb.hist + (epoch & 1u) * kSortPasses * kDigits;
+}
+
+__device__ __forceinline__ unsigned digit_of(unsigned long long key, int pass) {
+    return (unsigned)(key >> (8 * pass)) & 0xffu;
+}
+
+// The root above D path bits (the path's bits below 32 - D are zero).
+__device__ __forceinline__ unsigned long long pack_key(unsigned root, unsigned path, unsigned D) {
+    return D == 0 ? (unsigned long long)root : ((unsigned long long)root << D) | (path >> (32u - D));
+}
+
+// Lanes of the warp whose 8-bit digit equals this lane's (one ballot per
+// bit; valid = false lanes form a group of their own).
+__device__ __forceinline__ unsigned match_digit(unsigned d, bool valid) {
+    unsigned peers = __ballot_sync(0xffffffffu, valid);
+    if (!valid) peers = ~peers;
+#pragma unroll
+    for (int b = 0; b < 8; ++b) {
+        const unsigned bit = (d >> b) & 1u;
+        const unsigned m = __ballot_sync(0xffffffffu, bit);
+        peers &= bit ? m : ~m;
+    }
+    return peers;
+}
+
+// Bits of the frame's keys: the root bits of its root count above D path bits.
+__device__ __forceinline__ int key_bits(const unsigned long long* ctrl, unsigned* D_out) {
+    const unsigned long long R = *(volatile const unsigned long long*)(ctrl + kRoots * kCtrlStride);
+    unsigned D = (unsigned)*(volatile const unsigned long long*)(ctrl + kMaxDepth * kCtrlStride);
+    if (D > 32) D = 32;
+    if (D_out) *D_out = D;
+    const int root_bits = R > 1 ? 64 - __clzll((long long)(R - 1)) : 0;
+    return root_bits + (int)D;
+}
+
+// Keys, identity source slots, and the digit counts of the passes the keys
+// reach (warp-aggregated: one shared add per distinct digit of a warp's 32
+// keys); clears the next frame's counts, this frame's tile-group counts and
+// its published-tile counters.
+__global__ void __launch_bounds__(kKeysBlock) sort_keys_kernel(const int* __restrict__ root_prefix, SubPatches in,
+                                                               SortBuffers sb, unsigned long long* ctrl,
+                                                               int n_passes) {
+    __shared__ unsigned s_hist[kSortPasses][kDigits];
+    for (int i = threadIdx.x; i < kSortPasses * kDigits; i += kKeysBlock) (&s_hist[0][0])[i] = 0;
+    const unsigned epoch = frame_epoch(ctrl);
+    unsigned* next = hist_of(sb, epoch + 1);
+    const long long gt = (long long)blockIdx.x * kKeysBlock + threadIdx.x, gstride = (long long)gridDim.x * kKeysBlock;
+    for (long long i = gt; i < kSortPasses * kDigits; i += gstride) next[i] = 0;
+    for (long long i = gt; i < kSortPasses * sb.groups * kDigits; i += gstride) sb.group_counts[i] = 0;
+    if (blockIdx.x == 0 && threadIdx.x < kSortPasses) ctrl[(kSortTicket + threadIdx.x) * kCtrlStride] = 0;
+    __syncthreads();
+    const long long n = sort_count(ctrl, in, sb);
+    unsigned D = 0;
+    const int bits = key_bits(ctrl, &D);
+    const int active = (bits + 7) / 8 < n_passes ? (bits + 7) / 8 : n_passes;
+    const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
+    // whole warps step together so that the ballots below see every lane
+    for (long long base = (long long)blockIdx.x * kKeysBlock + (threadIdx.x & ~31); base < n; base += gstride) {
+        const long long i = base + lane;
+        const bool valid = i < n;
+        unsigned long long key = 0;
+        if (valid) {
+            const int2 m = in.meta[i];
+            const unsigned root = (unsigned)(__ldg(root_prefix + m.y) + m.x);
+            key = pack_key(root, in.path[i], D);
+            sb.keys[0][i] = key;
+            sb.vals[0][i] = (unsigned)i;
+        }
+        for (int p = 0; p < active; ++p) {
+            const unsigned d = digit_of(key, p);
+            const unsigned peers = match_digit(d, valid);
+            if (valid && (peers & lt) == 0) atomicAdd(&s_hist[p][d], (unsigned)__popc(peers));
+        }
+    }
+    __syncthreads();
+    unsigned* hist = hist_of(sb, epoch);
+    for (int i = threadIdx.x; i < active * kDigits; i += kKeysBlock) {
+        const unsigned v = (&s_hist[0][0])[i];
+        if (v) atomicAdd(hist + i, v);
+    }
+}
+
+// One radix pass.  Tile t (kSortTile keys) is block t % gridDim.x's, in
+// round t / gridDim.x; the grid is resident, and every block publishes its
+// tile's digit counts before it waits, so the waits end.  A tile's start in
+// digit bin d is the bin's start plus the counts of the earlier tiles, read
+// as the sums of whole groups of kSortGroup tiles (accumulated as tiles
+// publish) and the single counts of its own group's earlier tiles.  Warp w
+// of a tile owns the keys [tile * kSortTile + w * 32 * kSortItems, +32 *
+// kSortItems); item i of lane l is key i * 32 + l of that run, so a warp
+// ranks its run in key order and the pass is stable.  The last pass that
+// moves keys writes the records of `in` to `out` in their sorted order
+// instead of the keys.
+__global__ void __launch_bounds__(kSortBlock) sort_pass_kernel(SubPatches in, SubPatches out, SortBuffers sb,
+                                                               unsigned long long* ctrl, int pass, int n_passes,
+                                                               long long spin_limit) {
+    __shared__ unsigned s_wcount[kSortWarps][kDigits];   // per warp digit counts, then exclusive offsets
+    __shared__ unsigned s_start[kDigits];                // the pass's exclusive digit starts
+    __shared__ unsigned s_base[kDigits];                 // global start of each digit's run of this tile
+    __shared__ unsigned s_part[kDigits];                 // half of the earlier tiles' counts
+    __shared__ unsigned s_warp[kSortWarps];
+    __shared__ unsigned short s_rank[kSortItems][kSortBlock];   // rank of each item within its warp's run
+    __shared__ int s_fail;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const long long n = sort_count(ctrl, in, sb);
+    const unsigned epoch = frame_epoch(ctrl);
+    const unsigned* hist = hist_of(sb, epoch);
+    const int bits = key_bits(ctrl, nullptr);
+    const int active = (bits + 7) / 8 < n_passes ? (bits + 7) / 8 : n_passes;
+    // passes that move keys: those within the keys' bits whose digit is not
+    // the same for every key (the counts of all passes are loaded first)
+    unsigned h[kSortPasses];
+#pragma unroll
+    for (int q = 0; q < kSortPasses; ++q) h[q] = q < active && tid < kDigits ? hist[q * kDigits + tid] : 0u;
+    int moves_before = 0, moves_after = 0;
+    bool moves = false;
+#pragma unroll
+    for (int q = 0; q < kSortPasses; ++q) {
+        if (q >= active) break;
+        const int same = __syncthreads_or(tid < kDigits && (long long)h[q] == n);
+        if (!same) {
+            if (q < pass) ++moves_before;
+            else if (q == pass) moves = true;
+            else ++moves_after;
+        }
+    }
+    const long long stride = (long long)gridDim.x * kSortBlock;
+    if (!moves) {
+        // no pass moved anything (n <= 1): the records are already in order
+        if (pass == n_passes - 1 && moves_before == 0)
+            for (long long j = (long long)blockIdx.x * kSortBlock + tid; j < n && j < out.capacity; j += stride) {
+                out.range[j] = in.range[j];
+                out.meta[j] = in.meta[j];
+            }
+        return;
+    }
+    const bool last = moves_after == 0;
+    const int src = moves_before & 1;
+    // (selects, not an indexed load: the parameter arrays stay in registers)
+    const unsigned long long* __restrict__ kin = src ? sb.keys[1] : sb.keys[0];
+    const unsigned* __restrict__ vin = src ? sb.vals[1] : sb.vals[0];
+    unsigned long long* kout = src ? sb.keys[0] : sb.keys[1];
+    unsigned* vout = src ? sb.vals[0] : sb.vals[1];
+    unsigned* groups = sb.group_counts + (long long)pass * sb.groups * kDigits;
+    unsigned long long* published = ctrl + (kSortTicket + pass) * kCtrlStride;
+    if (tid < kDigits) {
+        // exclusive digit starts of this pass (warps 0-7)
+        const unsigned c = h[pass];
+        unsigned x = c;
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) s_warp[warp] = x;
+        s_start[tid] = x - c;
+    }
+    if (tid == 0) s_fail = 0;
+    __syncthreads();
+    if (tid < kDigits) {
+        unsigned before = 0;
+        for (int w = 0; w < warp; ++w) before += s_warp[w];
+        s_start[tid] += before;
+    }
+    const long long n_tiles = (n + kSortTile - 1) / kSortTile;
+    const unsigned lt = (1u << lane) - 1u;
+    for (long long tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
+        for (int i = tid; i < kSortWarps * kDigits; i += kSortBlock) (&s_wcount[0][0])[i] = 0;
+        __syncthreads();
+        const long long run = tile * kSortTile + (long long)warp * 32 * kSortItems;
+        unsigned long long k[kSortItems];
+        unsigned v[kSortItems];
+#pragma unroll
+        for (int i = 0; i < kSortItems; ++i) {
+            const long long idx = run + i * 32 + lane;
+            k[i] = idx < n ? __ldcg(kin + idx) : 0ull;
+            v[i] = idx < n ? __ldcg(vin + idx) : 0u;
+        }
+        unsigned* wc = s_wcount[warp];
+#pragma unroll
+        for (int i = 0; i < kSortItems; ++i) {
+            const bool valid = run + i * 32 + lane < n;
+            const unsigned d = digit_of(k[i], pass);
+            const unsigned peers = match_digit(d, valid);
+            const unsigned before = valid ? wc[d] : 0u;
+            s_rank[i][tid] = (unsigned short)(before + (unsigned)__popc(peers & lt));
+            __syncwarp();
+            if (valid && (peers & lt) == 0) wc[d] = before + (unsigned)__popc(peers);
+            __syncwarp();
+        }
+        __syncthreads();
+        if (tid < kDigits) {
+            // thread d: warp offsets within the tile and the tile's count, published
+            const int d = tid;
+            unsigned tot = 0;
+#pragma unroll
+            for (int w = 0; w < kSortWarps; ++w) {
+                const unsigned c = s_wcount[w][d];
+                s_wcount[w][d] = tot;
+                tot += c;
+            }
+            sb.counts[tile * kDigits + d] = tot;
+            if (tot) atomicAdd(groups + (tile / kSortGroup) * kDigits + d, tot);
+        }
+        __syncthreads();
+        if (tid == 0) {
+            // publish, then wait until every tile up to the end of this round has
+            __threadfence();
+            atomicAdd(published, 1ull);
+            const long long round_end = (tile / gridDim.x + 1) * gridDim.x;
+            const unsigned long long need = (unsigned long long)(round_end < n_tiles ? round_end : n_tiles);
+            long long spins = 0;
+            while (ld_acquire_u64(published) < need) {
+                if (++spins > spin_limit) {
+                    s_fail = 1;
+                    break;
+                }
+                __nanosleep(64);
+            }
+            __threadfence();
+        }
+        __syncthreads();
+        if (s_fail) {
+            // a wait ran out: report it and write nothing with a wrong base
+            if (tid == 0) set_status(ctrl, kErrTimeout);
+            return;
+        }
+        {
+            // counts of the earlier tiles, digit d: thread d adds the whole
+            // groups before this tile's group, thread d + 256 the earlier
+            // tiles of its own group
+            const int d = tid & (kDigits - 1);
+            const long long g = tile / kSortGroup;
+            unsigned sum = 0;
+            if (tid < kDigits) {
+                long long j = 0;
+                for (; j + 8 <= g; j += 8) {
+                    unsigned x[8];
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) x[u] = __ldcg(groups + (j + u) * kDigits + d);
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) sum += x[u];
+                }
+                for (; j < g; ++j) sum += __ldcg(groups + j * kDigits + d);
+            } else {
+                unsigned x[kSortGroup];
+#pragma unroll
+                for (int u = 0; u < kSortGroup; ++u)
+                    x[u] = g * kSortGroup + u < tile ? __ldcg(sb.counts + (g * kSortGroup + u) * kDigits + d) : 0u;
+#pragma unroll
+                for (int u = 0; u < kSortGroup; ++u) sum += x[u];
+                s_part[d] = sum;
+            }
+            __syncthreads();
+            if (tid < kDigits) s_base[d] = s_start[d] + sum + s_part[d];
+            __syncthreads();
+        }
+#pragma unroll
+        for (int i = 0; i < kSortItems; ++i) {
+            const long long idx = run + i * 32 + lane;
+            if (idx < n) {
+                const unsigned dg = digit_of(k[i], pass);
+                const long long dst = (long long)s_base[dg] + s_wcount[warp][dg] + s_rank[i][tid];
+                if (dst < n) {
+                    if (last) {
+                        if (dst < out.capacity && v[i] < (unsigned)n) {
+                            out.range[dst] = __ldcg(in.range + v[i]);
+                            out.meta[dst] = __ldcg(in.meta + v[i]);
+                        }
+                    } else {
+                        kout[dst] = k[i];
+                        vout[dst] = v[i];
+                    }
+                }
+            }
+        }
+        __syncthreads();
+    }
+}
+
+int sm_count() {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    return sms;
+}
+
+// Blocks resident at once (the pass's waits rely on it).
+int pass_grid() {
+    static int grid = 0;
+    if (grid == 0) {
+        int per_sm = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sort_pass_kernel, kSortBlock, 0);
+        grid = sm_count() * (per_sm < 1 ? 1 : per_sm);
+    }
+    return grid;
+}
+
+}  // namespace
+
+long long sort_tiles(long long n) { return (n + kSortTile - 1) / kSortTile; }
+
+int canonical_sort_passes(int max_split_depth, long long roots) {
+    // leaves lie at depth <= max_split_depth + 1; a path keeps 32 bits
+    const int path_bits = max_split_depth + 1 < 32 ? max_split_depth + 1 : 32;
+    int root_bits = 0;
+    while (root_bits < 32 && ((roots - 1) >> root_bits) > 0) ++root_bits;
+    const int bits = path_bits + root_bits;
+    return bits <= 8 ? 1 : (bits + 7) / 8;
+}
+
+void launch_canonical_sort(const int* root_prefix, const SubPatches& in, const SubPatches& out, const SortBuffers& sb,
+                           unsigned long long* ctrl, long long spin_limit, int n_passes, cudaStream_t s) {
+    sort_keys_kernel<<<sm_count(), kKeysBlock, 0, s>>>(root_prefix, in, sb, ctrl, n_passes);
+    const long long tiles = sb.tiles < 1 ? 1 : sb.tiles;
+    const int grid = (int)(tiles < pass_grid() ? tiles : pass_grid());
+    for (int p = 0; p < n_passes; ++p)
+        sort_pass_kernel<<<grid, kSortBlock, 0, s>>>(in, out, sb, ctrl, p, n_passes, spin_limit);
+}
+
+}  // namespace mp

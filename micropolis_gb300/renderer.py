@@ -216,8 +216,13 @@ class Renderer:
         self._ck(lib().mp_subpatches(self._ctx, ctypes.byref(cnt), _i32p(draw), _i32p(pid), _f32p(rng), n))
         return draw[:n], pid[:n], rng[:n]
 
-    STAGES = ("clear", "bound_split", "dice_raster", "raster_big", "resolve_or_shade", "sample", "pass_resolve",
-              "host_sync")
+    # mp_stats.stage_ms slots: the batched path fills clear, bound_split,
+    # canonical_sort_or_sample (its sort), dice_raster, raster_big and
+    # resolve_or_shade; the plain path bound_split, dice_raster (dice),
+    # resolve_or_shade (shade), canonical_sort_or_sample (sample),
+    # raster_big, pass_resolve and host_sync
+    STAGES = ("clear", "bound_split", "dice_raster", "raster_big", "resolve_or_shade", "canonical_sort_or_sample",
+              "pass_resolve", "host_sync")
 
     def stats(self) -> dict:
         s = MpStats()
@@ -243,6 +248,10 @@ class Renderer:
 
     def set_displacement_amplitude(self, amp: float) -> None:
         self._ck(lib().mp_set_displacement_amplitude(self._ctx, float(amp)))
+
+    def set_displacement_amplitude_device(self, dev_ptr: int) -> None:
+        """The amplitude multiplier from one float32 in device memory (stream-ordered copy)."""
+        self._ck(lib().mp_set_displacement_amplitude_device(self._ctx, ctypes.c_void_p(dev_ptr)))
 
     def set_grad_buffer(self, draw: int, dev_ptr: int) -> None:
         self._ck(lib().mp_set_grad_buffer(self._ctx, draw, ctypes.c_void_p(dev_ptr)))

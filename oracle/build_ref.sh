@@ -5,7 +5,8 @@
 # oracle/_ref/kernels/, outside the repository's history) with the CPU
 # work-item runtime ref_kernels.cpp, into oracle/_ref/libref_pin.so.  The reference's other
 # sources need OpenCL, OpenGL, GLFW, boost, capnp and generated config headers
-# and are not compiled.  Skips quietly when the reference tree is absent.
+# and are not compiled.  The tree is named by MP_REFERENCE_DIR; the script
+# skips quietly when that variable is unset or names no reference tree.
 #
 # The CPU sources compile without floating-point contraction (the reference's
 # CPU build on x86 has none).  The kernels compile with contraction on, as
@@ -13,7 +14,8 @@
 # gcc to emit fused multiply-adds, Arm has them in its base instruction set.
 set -e
 HERE=$(cd "$(dirname "$0")" && pwd)
-REF=${MP_REFERENCE_DIR:-/root/reference}
+REF=${MP_REFERENCE_DIR:-}
+[ -n "$REF" ] || { echo "build_ref: MP_REFERENCE_DIR is not set, skipped"; exit 0; }
 [ -f "$REF/src/base/Patch.cpp" ] || { echo "build_ref: no reference tree at $REF, skipped"; exit 0; }
 OUT="$HERE/_ref"
 mkdir -p "$OUT/obj"
@@ -36,4 +38,7 @@ g++ $COMMON $FMA -ffp-contract=fast -I "$HERE" -c "$HERE/ref_kernels.cpp" -o "$O
 for p in $PIDS; do wait "$p"; done
 g++ -shared -pthread -fopenmp "$OUT/obj/Patch.o" "$OUT/obj/Projection.o" "$OUT/obj/ref_pin.o" \
     "$OUT/obj/ref_kernels.o" "$OUT/obj/oracle.o" -o "$OUT/libref_pin.so"
+# where the pin came from, for the tests that read the reference's own files
+# (its test scenes, its trace tools) and skip where the tree is absent
+printf '%s\n' "$REF" > "$OUT/reference_dir.txt"
 echo "build_ref: $OUT/libref_pin.so"

@@ -184,7 +184,16 @@ struct PatchRange {
     float minx, miny, maxx, maxy;
     int64_t depth;
     int64_t patch_id;
+    // split path: bit 31 - d is 1 when the range is the high half of its
+    // depth-d ancestor's split (not in the reference's record; it names the
+    // range's place in the split tree for the canonical order below)
+    uint32_t path;
 };
+
+// Path of the high half of a split of r (the low half keeps r's path).
+static inline uint32_t high_path(const PatchRange& r) {
+    return r.depth < 32 ? r.path | (0x80000000u >> r.depth) : r.path;
+}
 
 // src/Reyes/BoundNSplitCLCPU.cpp:249-336 -- 3x3 samples at
 // min + (max-min)*i*0.5; v from range.x, u from range.y.
@@ -233,7 +242,7 @@ static int64_t bound_n_split(const or_params* P, const or_draw* d, Emit emit) {
     Projection proj;
     proj.init(P->fovy_deg, P->near_plane, P->width, P->height, P->cull_ribbon);
     std::vector<PatchRange> stack((size_t)d->n_patches);
-    for (int64_t i = 0; i < d->n_patches; ++i) stack[(size_t)i] = PatchRange{0, 0, 1, 1, 0, i};
+    for (int64_t i = 0; i < d->n_patches; ++i) stack[(size_t)i] = PatchRange{0, 0, 1, 1, 0, i, 0};
     const float s = P->bound_n_split_limit;
     int64_t bounds = 0;
     BBox box;
@@ -248,12 +257,12 @@ static int64_t bound_n_split(const or_params* P, const or_draw* d, Emit emit) {
                 emit(r);
             } else if (g == kGpuHSplit) {
                 float cy = (r.miny + r.maxy) * 0.5f;
-                stack.push_back(PatchRange{r.minx, r.miny, r.maxx, cy, r.depth + 1, r.patch_id});
-                stack.push_back(PatchRange{r.minx, cy, r.maxx, r.maxy, r.depth + 1, r.patch_id});
+                stack.push_back(PatchRange{r.minx, r.miny, r.maxx, cy, r.depth + 1, r.patch_id, r.path});
+                stack.push_back(PatchRange{r.minx, cy, r.maxx, r.maxy, r.depth + 1, r.patch_id, high_path(r)});
             } else if (g == kGpuVSplit) {
                 float cx = (r.minx + r.maxx) * 0.5f;
-                stack.push_back(PatchRange{r.minx, r.miny, cx, r.maxy, r.depth + 1, r.patch_id});
-                stack.push_back(PatchRange{cx, r.miny, r.maxx, r.maxy, r.depth + 1, r.patch_id});
+                stack.push_back(PatchRange{r.minx, r.miny, cx, r.maxy, r.depth + 1, r.patch_id, r.path});
+                stack.push_back(PatchRange{cx, r.miny, r.maxx, r.maxy, r.depth + 1, r.patch_id, high_path(r)});
             }
             continue;
         }
@@ -270,13 +279,13 @@ static int64_t bound_n_split(const or_params* P, const or_draw* d, Emit emit) {
         } else if (vlen < hlen) {
             // vsplit_range (:231-237): halve y, push low half then high half
             float cy = (r.miny + r.maxy) * 0.5f;
-            stack.push_back(PatchRange{r.minx, r.miny, r.maxx, cy, r.depth + 1, r.patch_id});
-            stack.push_back(PatchRange{r.minx, cy, r.maxx, r.maxy, r.depth + 1, r.patch_id});
+            stack.push_back(PatchRange{r.minx, r.miny, r.maxx, cy, r.depth + 1, r.patch_id, r.path});
+            stack.push_back(PatchRange{r.minx, cy, r.maxx, r.maxy, r.depth + 1, r.patch_id, high_path(r)});
         } else {
             // hsplit_range (:239-245): halve x
             float cx = (r.minx + r.maxx) * 0.5f;
-            stack.push_back(PatchRange{r.minx, r.miny, cx, r.maxy, r.depth + 1, r.patch_id});
-            stack.push_back(PatchRange{cx, r.miny, r.maxx, r.maxy, r.depth + 1, r.patch_id});
+            stack.push_back(PatchRange{r.minx, r.miny, cx, r.maxy, r.depth + 1, r.patch_id, r.path});
+            stack.push_back(PatchRange{cx, r.miny, r.maxx, r.maxy, r.depth + 1, r.patch_id, high_path(r)});
         }
     }
     return bounds;
@@ -884,6 +893,14 @@ extern "C" int or_render_subpatches(const or_params* p, const or_draw* draws, in
                                     int64_t n_sub, const int32_t* sub_draw, const int32_t* sub_pid,
                                     const float* sub_range, float* color, int32_t* depth,
                                     int64_t* win, int64_t* stats) {
+    return or_render_subpatches_at(p, draws, n_draws, n_sub, 0, sub_draw, sub_pid, sub_range, color, depth, win,
+                                   stats);
+}
+
+extern "C" int or_render_subpatches_at(const or_params* p, const or_draw* draws, int32_t n_draws, int64_t n_sub,
+                                       int64_t first_index, const int32_t* sub_draw, const int32_t* sub_pid,
+                                       const float* sub_range, float* color, int32_t* depth, int64_t* win,
+                                       int64_t* stats) {
     if (p->width % 8 || p->height % 8 || (p->reyes_patch_size % 8)) return 1;
     Frame f;
     f.init(p, color, depth, win);
@@ -891,7 +908,7 @@ extern "C" int or_render_subpatches(const or_params* p, const or_draw* draws, in
     for (int64_t s = 0; s < n_sub; ++s) {
         int dr = sub_draw ? sub_draw[s] : 0;
         if (dr < 0 || dr >= n_draws) return 2;
-        f.draw_subpatch(&draws[dr], sub_pid[s], sub_range + 4 * s, s * PS2);
+        f.draw_subpatch(&draws[dr], sub_pid[s], sub_range + 4 * s, (first_index + s) * PS2);
     }
     if (stats) {
         stats[0] = n_sub;
@@ -902,19 +919,72 @@ extern "C" int or_render_subpatches(const or_params* p, const or_draw* draws, in
     return 0;
 }
 
+// One emitted sub-patch of a frame with its canonical sort key.
+struct CanonicalSub {
+    uint64_t key;     // root << 32 | split path, root = draw's first root + patch id
+    int32_t draw;
+    int32_t pid;
+    float range[4];
+};
+
+// Every draw's sub-patches in the canonical order (ascending root, then
+// split path: each patch's split tree depth first, low half first), the
+// order in which the micropolygons of a frame are numbered.  Its first
+// argument the reference does not have: it emits in its stack's order
+// (src/Reyes/BoundNSplitCLCPU.cpp:75-159), which this sort puts in a form
+// that does not depend on how the work is scheduled.
+static std::vector<CanonicalSub> canonical_subpatches(const or_params* p, const or_draw* draws, int32_t n_draws,
+                                                      int64_t* n_bounds) {
+    std::vector<CanonicalSub> out;
+    uint64_t first_root = 0;
+    int64_t nb = 0;
+    for (int dr = 0; dr < n_draws; ++dr) {
+        nb += bound_n_split(p, &draws[dr], [&](const PatchRange& r) {
+            const uint64_t root = first_root + (uint64_t)r.patch_id;
+            out.push_back(CanonicalSub{(root << 32) | r.path, dr, (int32_t)r.patch_id, {r.minx, r.miny, r.maxx, r.maxy}});
+        });
+        first_root += (uint64_t)draws[dr].n_patches;
+    }
+    std::stable_sort(out.begin(), out.end(),
+                     [](const CanonicalSub& a, const CanonicalSub& b) { return a.key < b.key; });
+    if (n_bounds) *n_bounds = nb;
+    return out;
+}
+
+extern "C" int64_t or_canonical_subpatches(const or_params* p, const or_draw* draws, int32_t n_draws,
+                                           int32_t* draw, int32_t* pid, float* range, uint64_t* key, int64_t cap) {
+    const std::vector<CanonicalSub> subs = canonical_subpatches(p, draws, n_draws, nullptr);
+    for (int64_t i = 0; i < (int64_t)subs.size() && i < cap; ++i) {
+        if (draw) draw[i] = subs[(size_t)i].draw;
+        if (pid) pid[i] = subs[(size_t)i].pid;
+        if (range) std::memcpy(range + 4 * i, subs[(size_t)i].range, 4 * sizeof(float));
+        if (key) key[i] = subs[(size_t)i].key;
+    }
+    return (int64_t)subs.size();
+}
+
 extern "C" int or_render(const or_params* p, const or_draw* draws, int32_t n_draws, float* color,
                          int32_t* depth, int64_t* stats) {
+    return or_render_win(p, draws, n_draws, color, depth, nullptr, stats);
+}
+
+// The frame with its micropolygons numbered in the canonical order:
+// sub-patch s of canonical_subpatches() owns ids s * PS^2 + nu + nv * PS and,
+// drawn in that order with the first writer kept at equal depth, the
+// smallest id wins a tie.  win (may be NULL) receives the winning id of
+// every tiled pixel, or -1.
+extern "C" int or_render_win(const or_params* p, const or_draw* draws, int32_t n_draws, float* color,
+                             int32_t* depth, int64_t* win, int64_t* stats) {
     if (p->width % 8 || p->height % 8 || (p->reyes_patch_size % 8)) return 1;
     Frame f;
-    f.init(p, color, depth, nullptr);
+    f.init(p, color, depth, win);
     int64_t PS2 = (int64_t)p->reyes_patch_size * p->reyes_patch_size;
-    int64_t n_sub = 0, n_bounds = 0;
-    for (int dr = 0; dr < n_draws; ++dr) {
-        n_bounds += bound_n_split(p, &draws[dr], [&](const PatchRange& r) {
-            const float rg[4] = {r.minx, r.miny, r.maxx, r.maxy};
-            f.draw_subpatch(&draws[dr], (int32_t)r.patch_id, rg, n_sub * PS2);
-            ++n_sub;
-        });
+    int64_t n_bounds = 0;
+    const std::vector<CanonicalSub> subs = canonical_subpatches(p, draws, n_draws, &n_bounds);
+    const int64_t n_sub = (int64_t)subs.size();
+    for (int64_t s = 0; s < n_sub; ++s) {
+        const CanonicalSub& c = subs[(size_t)s];
+        f.draw_subpatch(&draws[c.draw], c.pid, c.range, s * PS2);
     }
     if (stats) {
         stats[0] = n_sub;

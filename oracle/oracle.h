@@ -64,12 +64,26 @@ typedef struct {
 int64_t or_bound_n_split(const or_params* p, const or_draw* d,
                          int32_t* pid, float* range, int64_t cap, int64_t* n_bounds);
 
-/* Full frame: clear, then for every draw bound-and-split, dice, shade and
- * sample in emission order.  color: tiled float4 framebuffer (W*H*4),
- * depth: tiled int32 depth buffer (W*H).  stats (may be NULL) receives
- * [sub-patches, micropolygons, fragments, bounds]. */
+/* Every draw's sub-patches in the canonical order: ascending key
+ * (root << 32 | split path), root = the draw's first root + patch id (draws
+ * in order), the split path's bit 31 - d set when the sub-patch is the high
+ * half of its depth-d ancestor's split.  Writes up to cap records (any output
+ * may be NULL) and returns how many there are. */
+int64_t or_canonical_subpatches(const or_params* p, const or_draw* draws, int32_t n_draws,
+                                int32_t* draw, int32_t* pid, float* range, uint64_t* key, int64_t cap);
+
+/* Full frame: clear, bound-and-split every draw, then dice, shade and
+ * sample the sub-patches in the canonical order, numbering micropolygons
+ * s * PS^2 + nu + nv * PS for canonical sub-patch s; at equal depth the
+ * first writer (the smallest number) is kept.  color: tiled float4
+ * framebuffer (W*H*4), depth: tiled int32 depth buffer (W*H).  stats (may be
+ * NULL) receives [sub-patches, micropolygons, fragments, bounds]. */
 int or_render(const or_params* p, const or_draw* draws, int32_t n_draws,
               float* color, int32_t* depth, int64_t* stats);
+/* Same, and win (may be NULL) receives the winning number of every tiled
+ * pixel, or -1. */
+int or_render_win(const or_params* p, const or_draw* draws, int32_t n_draws,
+                  float* color, int32_t* depth, int64_t* win, int64_t* stats);
 
 /* Same, but from an explicit sub-patch list (draw index, pid, range), so that
  * the kernel restatement can be checked on a given set.  win (may be NULL)
@@ -79,6 +93,13 @@ int or_render_subpatches(const or_params* p, const or_draw* draws, int32_t n_dra
                          int64_t n_sub, const int32_t* sub_draw, const int32_t* sub_pid,
                          const float* sub_range, float* color, int32_t* depth,
                          int64_t* win, int64_t* stats);
+/* Same, with the list's sub-patch s numbered first_index + s (a slice of a
+ * longer list: slices merged by the smallest (depth, number) per pixel give
+ * the frame of the whole list). */
+int or_render_subpatches_at(const or_params* p, const or_draw* draws, int32_t n_draws, int64_t n_sub,
+                            int64_t first_index, const int32_t* sub_draw, const int32_t* sub_pid,
+                            const float* sub_range, float* color, int32_t* depth, int64_t* win,
+                            int64_t* stats);
 
 /* Restated dice of one sub-patch: (PS+1)^2 vertices, index nu + nv*(PS+1).
  * pos: float4 eye-space (after displacement), pxl: int2, depth: float. */

@@ -60,6 +60,16 @@ def lib():
         L.or_render.restype = ctypes.c_int
         L.or_render.argtypes = [ctypes.POINTER(OrParams), ctypes.POINTER(OrDraw), ctypes.c_int32, f32p,
                                 i32p, i64p]
+        L.or_render_win.restype = ctypes.c_int
+        L.or_render_win.argtypes = [ctypes.POINTER(OrParams), ctypes.POINTER(OrDraw), ctypes.c_int32, f32p,
+                                    i32p, i64p, i64p]
+        L.or_canonical_subpatches.restype = ctypes.c_int64
+        L.or_canonical_subpatches.argtypes = [ctypes.POINTER(OrParams), ctypes.POINTER(OrDraw), ctypes.c_int32,
+                                              i32p, i32p, f32p, ctypes.POINTER(ctypes.c_uint64), ctypes.c_int64]
+        L.or_render_subpatches_at.restype = ctypes.c_int
+        L.or_render_subpatches_at.argtypes = [ctypes.POINTER(OrParams), ctypes.POINTER(OrDraw), ctypes.c_int32,
+                                              ctypes.c_int64, ctypes.c_int64, i32p, i32p, f32p, f32p, i32p, i64p,
+                                              i64p]
         L.or_render_subpatches.restype = ctypes.c_int
         L.or_render_subpatches.argtypes = [ctypes.POINTER(OrParams), ctypes.POINTER(OrDraw), ctypes.c_int32,
                                            ctypes.c_int64, i32p, i32p, f32p, f32p, i32p, i64p, i64p]
@@ -139,20 +149,89 @@ def bound_n_split(scene, draw_index=0, params=None, cap=None):
     return pid[:n], rng[:n], int(n_b.value)
 
 
-def render(scene, params=None, draws=None):
-    """Full frame: (tiled colour float32[W*H,4], tiled depth int32[W*H], stats dict)."""
+def render(scene, params=None, draws=None, want_win=False):
+    """Full frame with micropolygons numbered in the canonical order:
+    (tiled colour float32[W*H,4], tiled depth int32[W*H], stats dict), and
+    with want_win the winning micropolygon number of every tiled pixel
+    (int64, -1 where none) before the stats."""
     p = params or make_params(scene)
     draws = scene.draws if draws is None else draws
     ds = _Draws(draws)
     npx = scene.width * scene.height
     color = np.zeros((npx, 4), np.float32)
     depth = np.zeros(npx, np.int32)
+    win = np.zeros(npx, np.int64) if want_win else None
     st = np.zeros(4, np.int64)
-    rc = lib().or_render(ctypes.byref(p), ds.arr, ds.n, _ptr(color, f32p), _ptr(depth, i32p), _ptr(st, i64p))
+    rc = lib().or_render_win(ctypes.byref(p), ds.arr, ds.n, _ptr(color, f32p), _ptr(depth, i32p),
+                             _ptr(win, i64p) if want_win else None, _ptr(st, i64p))
     if rc:
         raise ValueError(f"oracle render failed: {rc}")
-    return color, depth, dict(subpatches=int(st[0]), micropolygons=int(st[1]), fragments=int(st[2]),
-                              bounds=int(st[3]))
+    stats = dict(subpatches=int(st[0]), micropolygons=int(st[1]), fragments=int(st[2]), bounds=int(st[3]))
+    return (color, depth, win, stats) if want_win else (color, depth, stats)
+
+
+def canonical_subpatches(scene, params=None):
+    """Every draw's sub-patches in the canonical order (ascending root, then
+    split path): (draw int32[S], pid int32[S], range float32[S,4], key uint64[S])."""
+    p = params or make_params(scene)
+    ds = _Draws(scene.draws)
+    n = lib().or_canonical_subpatches(ctypes.byref(p), ds.arr, ds.n, None, None, None, None, 0)
+    m = max(n, 1)
+    draw = np.zeros(m, np.int32)
+    pid = np.zeros(m, np.int32)
+    rng = np.zeros((m, 4), np.float32)
+    key = np.zeros(m, np.uint64)
+    lib().or_canonical_subpatches(ctypes.byref(p), ds.arr, ds.n, _ptr(draw, i32p), _ptr(pid, i32p), _ptr(rng, f32p),
+                                  key.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)), n)
+    return draw[:n], pid[:n], rng[:n], key[:n]
+
+
+def _render_slice(args):
+    """One process's share of render_parallel: the canonical sub-patches
+    [first, first + len) of the frame, numbered from first."""
+    scene, params_over, first, sdraw, spid, srange = args
+    p = make_params(scene, **params_over)
+    ds = _Draws(scene.draws)
+    npx = scene.width * scene.height
+    color = np.zeros((npx, 4), np.float32)
+    depth = np.zeros(npx, np.int32)
+    win = np.zeros(npx, np.int64)
+    st = np.zeros(4, np.int64)
+    sd = np.ascontiguousarray(sdraw, np.int32)
+    sp = np.ascontiguousarray(spid, np.int32)
+    sr = np.ascontiguousarray(srange, np.float32).reshape(-1)
+    rc = lib().or_render_subpatches_at(ctypes.byref(p), ds.arr, ds.n, len(sp), int(first), _ptr(sd, i32p),
+                                       _ptr(sp, i32p), _ptr(sr, f32p), _ptr(color, f32p), _ptr(depth, i32p),
+                                       _ptr(win, i64p), _ptr(st, i64p))
+    if rc:
+        raise ValueError(f"oracle render failed: {rc}")
+    return color, depth, win, int(st[2])
+
+
+def render_parallel(scene, pool, params_over=None, slices=None):
+    """The frame of render(scene, want_win=True), computed by `pool`
+    (multiprocessing, spawn context) over slices of the canonical list and
+    merged by the smallest (depth, micropolygon number) per pixel -- the rule
+    one sequential pass keeps, so the merge is exact."""
+    params_over = params_over or {}
+    p = make_params(scene, **params_over)
+    draw, pid, rng, _ = canonical_subpatches(scene, p)
+    n = len(pid)
+    k = max(1, min(slices or getattr(pool, "_processes", 1) * 4, n))
+    bounds = [n * i // k for i in range(k + 1)]
+    jobs = [(scene, params_over, bounds[i], draw[bounds[i]:bounds[i + 1]], pid[bounds[i]:bounds[i + 1]],
+             rng[bounds[i]:bounds[i + 1]]) for i in range(k)]
+    parts = pool.map(_render_slice, jobs)
+    color, depth, win, frags = parts[0][0].copy(), parts[0][1].copy(), parts[0][2].copy(), parts[0][3]
+    for c, d, w, f in parts[1:]:
+        # pixels of a later slice replace only at smaller depth, or equal depth and smaller number
+        take = (d < depth) | ((d == depth) & (w >= 0) & ((win < 0) | (w < win)))
+        color[take] = c[take]
+        depth[take] = d[take]
+        win[take] = w[take]
+        frags += f
+    stats = dict(subpatches=n, micropolygons=n * p.reyes_patch_size ** 2, fragments=frags)
+    return color, depth, win, stats
 
 
 def render_subpatches(scene, sub_draw, sub_pid, sub_range, params=None, want_win=False):
@@ -238,6 +317,17 @@ def inclusive_scan(a):
 
 
 # --- reference pin (only where the reference tree was compiled) -------------
+
+def reference_dir():
+    """The reference tree the pin was built from (MP_REFERENCE_DIR, else the
+    directory build_ref.sh recorded), or None where it is not present."""
+    d = os.environ.get("MP_REFERENCE_DIR")
+    if not d:
+        rec = os.path.join(HERE, "_ref", "reference_dir.txt")
+        if os.path.exists(rec):
+            d = open(rec).read().strip()
+    return d if d and os.path.isdir(d) else None
+
 
 _ref = None
 

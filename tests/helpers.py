@@ -81,3 +81,50 @@ def golden_gpucrit(name):
     import os
     z = np.load(os.path.join(GOLDEN_DIR, "gpucrit_" + name + ".npz"))
     return z["pid"], z["range"]
+
+
+def same_colour(a, b):
+    """Per-pixel bit equality of two float colour arrays (any two NaNs agree)."""
+    a, b = np.asarray(a, np.float32), np.asarray(b, np.float32)
+    same = (a.view(np.uint32) == b.view(np.uint32)) | (np.isnan(a) & np.isnan(b))
+    return np.all(same, axis=-1)
+
+
+def assert_identical_to_oracle(r, scene, params=None, oracle_frame=None):
+    """A batched frame against the oracle's frame of the same scene: the
+    sub-patch list equal to the oracle's canonical list in order and bit for
+    bit, colour and depth bit-identical at every pixel, and the same winning
+    micropolygon number at every pixel (ties included: both number
+    micropolygons in the canonical order and keep the smallest at equal
+    depth).  oracle_frame: (colour, depth, winners, stats) when already
+    rendered (oracle.render_parallel).  Returns the oracle's stats."""
+    from oracle import oracle
+    p = params or oracle.make_params(scene)
+    odraw, opid, orng, _ = oracle.canonical_subpatches(scene, p)
+    draw, pid, rng = r.subpatches()
+    assert len(pid) == len(opid), (len(pid), len(opid))
+    assert np.array_equal(draw, odraw) and np.array_equal(pid, opid)
+    assert np.array_equal(np.ascontiguousarray(rng, np.float32).view(np.uint32),
+                          np.ascontiguousarray(orng, np.float32).view(np.uint32))
+    if oracle_frame is None:
+        oracle_frame = oracle.render(scene, params=p, want_win=True)
+    ocol, odep, owin, ost = oracle_frame
+    col, dep = r.read_framebuffer()
+    assert np.array_equal(dep, odep), int(np.count_nonzero(dep != odep))
+    same = same_colour(col, ocol)
+    assert same.all(), int(np.count_nonzero(~same))
+    vis = r.visibility()
+    assert np.array_equal(vis, owin), int(np.count_nonzero(vis != owin))
+    st = r.stats()
+    assert st["micropolygons"] == ost["micropolygons"] and st["fragments"] == ost["fragments"]
+    return ost
+
+
+def sort_passes(max_split_depth, roots):
+    """Radix passes the batched frame launches for its canonical order: 8-bit
+    digits of root bits (up to roots - 1) above at most min(32,
+    max_split_depth + 1) path bits."""
+    path_bits = min(32, max_split_depth + 1)
+    root_bits = int(roots - 1).bit_length() if roots > 1 else 0
+    bits = path_bits + root_bits
+    return 1 if bits <= 8 else (bits + 7) // 8

@@ -104,19 +104,20 @@ def test_overflow_regrowth(built, cuda):
     _check(sc, "batched", queue_capacity=256, subpatch_capacity=16)
 
 
-def test_bounded_wait_reports_timeout(built, cuda):
-    """With a spin limit of one iteration the persistent bound-and-split gives
-    up waiting and reports MP_ERR_TIMEOUT (or finishes); it never hangs, and
-    the device stays usable."""
+@pytest.mark.parametrize("overlap", [0, 1])
+def test_bounded_wait_reports_timeout(built, cuda, overlap):
+    """With a spin limit of one iteration the waits run out: the grid holds
+    far more tickets than the scene has ranges, so warps whose tickets are
+    never filled check twice, 32 ns apart, long before bound-and-split ends
+    (the overlapped kernel's raster blocks likewise wait for slots).  The
+    frame reports MP_ERR_TIMEOUT instead of hanging and rasterizes nothing of
+    its incomplete list; a fresh context renders the scene correctly."""
     from micropolis_gb300 import _lib
     sc = _small_scene(n=512)
-    try:
-        _render(sc, "batched", spin_limit=1).close()
-        status = 0
-    except _lib.MpError as e:
-        status = e.status
-    assert status in (_lib.MP_OK, _lib.MP_ERR_TIMEOUT)
-    _check(sc, "batched")   # a fresh context still renders correctly
+    with pytest.raises(_lib.MpError) as e:
+        _render(sc, "batched", spin_limit=1, overlap=overlap)
+    assert e.value.status == _lib.MP_ERR_TIMEOUT
+    _check(sc, "batched")
 
 
 def test_dice16(built, cuda):

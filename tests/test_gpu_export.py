@@ -8,7 +8,7 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 # command names the reference's tools/trace_summary.py maps
-TRACE_NAMES = {"sample", "dice", "shade", "bound & split", "clear framebuffer"}
+TRACE_NAMES = {"sample", "dice", "shade", "bound & split", "clear framebuffer", "accumulate"}
 
 
 def _scene():
@@ -65,5 +65,16 @@ def test_trace_and_stats_formats(built, cuda, path):
     assert s["max_patches"] > 0 and s["opengl_mem"] == 0
     r.set_stage_timing(False)
     render_scene(r, sc)
-    assert oracle.parse_trace(r.dump_trace())[0][0] == "frame"
+    if path == "batched":
+        # the frame's graph records its stage events: same lines without stage timing
+        items = oracle.parse_trace(r.dump_trace())
+        assert [it[0] for it in items] == ["clear framebuffer", "bound & split", "accumulate", "dice", "sample",
+                                           "shade"]
+        assert all(it[5] >= it[4] >= 0 for it in items)
+        assert abs(sum(r.stats()["stage_ms"].values()) - sum(it[5] - it[4] for it in items) / 1e6) < 1e-3
+    else:
+        from micropolis_gb300 import _lib
+        with pytest.raises(_lib.MpError) as e:
+            r.dump_trace()
+        assert e.value.status == _lib.MP_ERR_STATE
     r.close()

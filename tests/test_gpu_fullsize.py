@@ -1,11 +1,27 @@
-"""Full-size workloads, checked through properties that do not need the CPU
-to render the frame: bit-exact sub-patch sets against the oracle's
-bound-and-split, batched path equal to the plain per-pass path, determinism,
-micropolygon counts, and dyadic ranges inside [0,1]^2."""
+"""Full-size workloads: the headline mixed scene's whole frame, four of the
+64 views at their full patch counts and a crop of the 4K displaced
+heightfield, each bit-identical to the oracle (colour, depth, winning
+micropolygon); and properties the whole frames keep: bit-exact sub-patch
+sets against the oracle's bound-and-split, batched path equal to the plain
+per-pass path, determinism, micropolygon counts, and dyadic ranges inside
+[0,1]^2."""
+import os
+
 import numpy as np
 import pytest
 
-from helpers import framebuffer_diff, subpatch_set
+from helpers import assert_identical_to_oracle, framebuffer_diff, same_colour, subpatch_set
+
+
+@pytest.fixture(scope="module")
+def pool():
+    """Oracle worker processes (spawned: never forked from a process that
+    has touched the GPU)."""
+    import multiprocessing as mp
+    p = mp.get_context("spawn").Pool(min(16, os.cpu_count() or 1))
+    yield p
+    p.close()
+    p.join()
 
 
 def _sorted_records(pid, rng, draw=None):
@@ -62,14 +78,124 @@ def test_mixed4096_full_size(built, cuda):
     cp_, zp = rp.read_framebuffer()
     bad, _ = framebuffer_diff(cb, zb, cp_, zp, REL_TOL)
     assert bad <= COVERAGE_BUDGET * zb.size
-    # a second frame renders the same image
+    # a second frame renders the same image, bit for bit
     from micropolis_gb300.renderer import render_scene
     render_scene(rb, sc)
     cb2, zb2 = rb.read_framebuffer()
-    bad, _ = framebuffer_diff(cb, zb, cb2, zb2, REL_TOL)
-    assert bad <= COVERAGE_BUDGET * zb.size
+    assert np.array_equal(zb, zb2) and same_colour(cb, cb2).all()
     rb.close()
     rp.close()
+
+
+def test_mixed4096_frame_identical_to_oracle(built, cuda, pool):
+    """The headline frame (4,096 mixed patches, 1920x1080, limit 8, dice
+    8x8): canonical sub-patch list, colour, depth and visibility
+    bit-identical to the oracle's frame at every pixel."""
+    from micropolis_gb300 import scenes
+    from oracle import oracle
+    sc = scenes.mixed4096_1920x1080()
+    r = _render(sc, "batched")
+    frame = oracle.render_parallel(sc, pool)
+    assert_identical_to_oracle(r, sc, oracle.make_params(sc), frame)
+    r.close()
+
+
+def test_views64_four_layers_identical_to_oracle(built, cuda):
+    """The 64-view frame at full patch counts: four of its layers, each
+    against the oracle's frame of that view's draw alone (its micropolygon
+    numbers offset by the sub-patches of the earlier draws)."""
+    from micropolis_gb300 import scenes
+    from oracle import oracle
+    sc = scenes.views64_512x512()
+    r = _render(sc, "batched")
+    draw, pid, rng = r.subpatches()
+    counts = np.bincount(draw, minlength=len(sc.draws))
+    first = np.concatenate([[0], np.cumsum(counts)[:-1]])
+    for v in (0, 21, 42, 63):
+        d = sc.draws[v]
+        one = scenes.Scene(sc.name, sc.width, sc.height, [scenes.Draw(d.mesh, d.mv, d.color, 0)], fovy=sc.fovy,
+                           near=sc.near, options={k: x for k, x in sc.options.items() if k != "batch_views"})
+        p = oracle.make_params(one)
+        odraw, opid, orng, _ = oracle.canonical_subpatches(one, p)
+        sl = slice(first[v], first[v] + counts[v])
+        assert np.array_equal(pid[sl], opid)
+        assert np.array_equal(rng[sl].view(np.uint32), orng.view(np.uint32))
+        ocol, odep, owin, _ = oracle.render(one, params=p, want_win=True)
+        col, dep = r.read_framebuffer(view=v)
+        assert np.array_equal(dep, odep) and same_colour(col, ocol).all(), v
+        vis = r.visibility(view=v)
+        want = np.where(owin >= 0, owin + first[v] * 64, -1)
+        assert np.array_equal(vis, want), v
+    r.close()
+
+
+def _crop_patches(scene, x0, y0, x1, y1, margin_px=4):
+    """Patches whose displaced surface can reach pixels [x0, x1) x [y0, y1):
+    the eye-space box of the control points (a Bezier patch lies in their
+    convex hull) grown by the largest displacement (0.07 x amplitude per
+    coordinate, kernels/dice.cl:51-67), projected through its corners; boxes
+    reaching the eye plane are kept."""
+    d = scene.draws[0]
+    mv = np.asarray(d.mv, np.float64).reshape(4, 4).T
+    cp = d.mesh.cp.astype(np.float64)
+    eye = cp @ mv[:3, :3].T + mv[:3, 3]
+    amp = float(scene.options.get("displacement_amplitude", 1.0)) if scene.options.get("displacement") else 0.0
+    m = 0.07 * abs(amp) * 1.01 + 1e-6
+    lo, hi = eye.min(axis=1) - m, eye.max(axis=1) + m
+    keep = hi[:, 2] >= -scene.near
+    f = 1.0 / np.tan(np.radians(scene.fovy) / 2)
+    aspect = scene.width / scene.height
+    corners = np.stack([np.stack([np.where(k & 1, hi[:, 0], lo[:, 0]), np.where(k & 2, hi[:, 1], lo[:, 1]),
+                                  np.where(k & 4, hi[:, 2], lo[:, 2])], -1) for k in range(8)], 1)
+    w = -corners[:, :, 2]
+    with np.errstate(divide="ignore", invalid="ignore"):
+        px = (f / aspect) * corners[:, :, 0] / w * scene.width / 2 + scene.width / 2
+        py = f * corners[:, :, 1] / w * scene.height / 2 + scene.height / 2
+    hit = (px.min(1) <= x1 + margin_px) & (px.max(1) >= x0 - margin_px) & \
+          (py.min(1) <= y1 + margin_px) & (py.max(1) >= y0 - margin_px)
+    return np.nonzero(keep | hit)[0]
+
+
+def test_heightfield512_4k_crop_identical_to_oracle(built, cuda, pool):
+    """A 256x256-pixel crop of the 262,144-patch displaced heightfield at
+    3840x2160 (limit 4 px): colour, depth and the winning micropolygon's
+    identity (patch, range, quad) at every crop pixel equal the oracle's
+    frame of the patches that can reach the crop."""
+    from micropolis_gb300 import scenes
+    from oracle import oracle
+    sc = scenes.heightfield512_3840x2160()
+    r = _render(sc, "batched")
+    col, dep = r.read_framebuffer(linear=True)
+    vis_t = r.visibility()
+    draw, pid, rng = r.subpatches()
+    x0, y0, x1, y1 = 1792, 952, 2048, 1208
+    sel = _crop_patches(sc, x0, y0, x1, y1)
+    assert 0 < len(sel) < sc.n_patches // 4
+    d = sc.draws[0]
+    sub = scenes.Scene(sc.name, sc.width, sc.height, [scenes.Draw(scenes.Mesh(d.mesh.type, d.mesh.cp[sel]), d.mv,
+                                                                  d.color)],
+                       fovy=sc.fovy, near=sc.near, options=dict(sc.options))
+    p = oracle.make_params(sub)
+    _, opid, orng, _ = oracle.canonical_subpatches(sub, p)
+    ocol_t, odep_t, owin_t, _ = oracle.render_parallel(sub, pool)
+    # tiled -> row-major for the crop
+    W, H = sc.width, sc.height
+    yy, xx = np.mgrid[y0:y1, x0:x1]
+    tiled = ((xx // 8) + (W // 8) * (yy // 8)) * 64 + (xx % 8) + 8 * (yy % 8)
+    lin = yy * W + xx
+    assert np.array_equal(dep[lin], odep_t[tiled])
+    assert same_colour(col[lin], ocol_t[tiled]).all()
+    g = vis_t[tiled]
+    o = owin_t[tiled]
+    assert np.array_equal(g >= 0, o >= 0)
+    covered = g >= 0
+    assert covered.mean() > 0.5
+    gs, gq = g[covered] // 64, g[covered] % 64
+    os_, oq = o[covered] // 64, o[covered] % 64
+    assert np.array_equal(gq, oq)
+    assert np.array_equal(pid[gs], sel[opid[os_]])
+    assert np.array_equal(rng[gs].view(np.uint32), orng[os_].view(np.uint32))
+    r.close()
 
 
 def test_heightfield512_4k_full_size(built, cuda):

@@ -4,7 +4,7 @@ sub-patch set, fragment count and image as the oracle."""
 import numpy as np
 import pytest
 
-from helpers import framebuffer_diff, subpatch_set
+from helpers import assert_identical_to_oracle, framebuffer_diff, sort_passes, subpatch_set
 
 pytestmark = pytest.mark.gpu
 
@@ -32,18 +32,31 @@ def _oracle(sc):
 
 @pytest.mark.parametrize("ps,groups", [(8, (8, 11, 16, 22)), (16, (2, 3, 4, 6))])
 def test_knobs_match_oracle(built, cuda, ps, groups):
+    """Every knob setting renders the oracle's frame: bit-identical (list
+    order, colour, depth, visibility) in separate launches; the same
+    sub-patch set and fragments, and pixels within the tie budget, with the
+    overlapped kernel, whose numbering follows the emission order."""
     from micropolis_gb300.renderer import render_scene, renderer_for
+    from oracle import oracle
     sc = _scene(ps)
     want, ocol, odep, ost = _oracle(sc)
+    frame = oracle.render(sc, params=oracle.make_params(sc), want_win=True)
+    passes = sort_passes(23, sc.n_patches)
     for tile in (8, 16, 32):
         for group in groups:
             for overlap in (False, True):
                 r = renderer_for(sc, "batched", raster_tile=tile, dice_group=group, overlap=overlap)
                 render_scene(r, sc)
+                if not overlap:
+                    assert_identical_to_oracle(r, sc, oracle.make_params(sc), frame)
+                    # clear, bound-and-split, sort keys, sort passes, dice+raster, slow raster, resolve
+                    assert r.stats()["kernels"] == 6 + passes
+                    r.close()
+                    continue
                 d, p, g = r.subpatches()
                 assert subpatch_set(p, g, d) == want, (tile, group, overlap)
                 assert r.stats()["fragments"] == ost["fragments"], (tile, group, overlap)
-                assert r.stats()["kernels"] == (4 if overlap else 5)
+                assert r.stats()["kernels"] == 4
                 col, dep = r.read_framebuffer()
                 bad, _ = framebuffer_diff(col, dep, ocol, odep, REL_TOL)
                 assert bad <= COVERAGE_BUDGET * dep.size, (tile, group, overlap, bad)

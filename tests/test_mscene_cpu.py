@@ -8,9 +8,16 @@ import pytest
 
 from micropolis_gb300 import _lib, mscene, scenes
 
-# the reference's packed scenes, where its tree is present (the same
-# variable oracle/build_ref.sh reads)
-REF_SCENES = os.path.join(os.environ.get("MP_REFERENCE_DIR", "/root/reference"), "testscene")
+
+def _ref_scenes():
+    """The reference's packed scenes, where its tree is present (the one
+    oracle/build_ref.sh compiled the pin from)."""
+    from oracle import oracle
+    d = oracle.reference_dir()
+    return os.path.join(d, "testscene") if d else ""
+
+
+REF_SCENES = _ref_scenes()
 
 
 def _records():
