@@ -249,10 +249,11 @@ mp_status mp_inclusive_scan(mp_ctx* ctx, const int32_t* host_in, int32_t* host_o
  * library.  n may be at most 4,194,304 (MP_ERR_INVALID_ARG beyond).  The
  * first call on a device looks up that array's device address, so make it
  * before any stream capture.  All calls on a device share the array: calls
- * that overlap on the GPU race and must be serialized by the caller.  Runs on
- * `stream` (a cudaStream_t, NULL = default stream) and returns when the scan
- * is done: it synchronizes `stream` and reads the scan's status word back to
- * the host (MP_ERR_TIMEOUT when a bounded wait gave up). */
+ * that overlap on the GPU race and must be serialized by the caller.  Every
+ * call is blocking: it runs on `stream` (a cudaStream_t, NULL = default
+ * stream), then waits for that stream (cudaStreamSynchronize) and copies the
+ * scan's status word to host memory before it returns (MP_ERR_TIMEOUT when a
+ * bounded wait gave up). */
 mp_status mp_inclusive_scan_noalloc(const int32_t* in_dev, int32_t* out_dev, int64_t n, void* stream);
 
 /* The image the reference shows for one layer (shaders/tex_draw.frag: gamma

@@ -139,3 +139,27 @@ def test_prefix_sum_reference_selftest(built, cuda):
         out = r.inclusive_scan(vals)
         assert np.array_equal(out, np.cumsum(vals, dtype=np.int64).astype(np.int32))
         r.close()
+
+
+def test_gregory_form_dices_to_the_bezier_surface(built, cuda):
+    """Known answer of tools/bez2mscene_greg.py:111 on the CUDA dicer: a
+    Bezier patch and its 20-point Gregory form dice to the same surface
+    (within a few FP32 roundings), and each form's grid is bit-exact to the
+    oracle's."""
+    from oracle import oracle
+    from test_bez2greg_cpu import RANGES, REL_TOL, bezier_and_gregory_scene
+    sc = bezier_and_gregory_scene()
+    r = _render(sc, "batched")
+    n = sc.draws[0].mesh.n_patches
+    pid = np.repeat(np.arange(n, dtype=np.int32), len(RANGES))
+    rng = np.tile(RANGES, (n, 1))
+    pb, xb, db = r.dice_subpatches(0, pid, rng)
+    pg, xg, dg = r.dice_subpatches(1, pid, rng)
+    for k in range(len(pid)):
+        scale = np.abs(pb[k, :, :3]).max()
+        assert np.abs(pg[k, :, :3] - pb[k, :, :3]).max() <= REL_TOL * scale, k
+        assert np.abs(xg[k] - xb[k]).max() <= 1
+        for draw, pos, pxl, dep in ((0, pb, xb, db), (1, pg, xg, dg)):
+            opos, opxl, odep = oracle.dice(sc, draw, pid[k], rng[k])
+            assert np.array_equal(pos[k], opos) and np.array_equal(pxl[k], opxl) and np.array_equal(dep[k], odep)
+    r.close()
