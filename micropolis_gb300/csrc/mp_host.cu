@@ -96,7 +96,7 @@ struct mp_ctx {
     // cannot tell that the captured sizes and pointers are stale
     bool graph_stale = false;
 
-    int bns_grid = 0, raster_grid = 0, frame_grid = 0;
+    int bns_grid = 0, raster_grid = 0, frame_grid = 0, sort_grid = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     bool stage_timing = false;
     void* staging = nullptr;          // pinned upload buffer (xyz of pageable sources)
@@ -471,7 +471,7 @@ long long batched_kernels(const mp_ctx* c) {
 
 void launch_sort(mp_ctx* c) {
     launch_canonical_sort(c->d_root_prefix, c->sub, c->sorted, c->sb, c->ctrl, c->opt.spin_limit, c->sort_passes,
-                          c->stream);
+                          c->sort_grid, c->stream);
 }
 
 // Stages of a batched frame in launch order: the mp_stats.stage_ms slot
@@ -800,6 +800,7 @@ mp_status mp_create(const mp_options* opts, mp_ctx** out) {
         c->bns_grid = bns_persistent_grid(fr.criterion);
         c->raster_grid = raster_fused_grid(fr.PS, o.dice_group);
         c->frame_grid = frame_kernel_grid(fr.PS, o.dice_group);
+        c->sort_grid = canonical_sort_grid();
         launch_clear(c->fb, c->fr, 1, c->stream);
         ck(cudaStreamSynchronize(c->stream), "init");
     }

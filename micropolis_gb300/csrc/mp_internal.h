@@ -68,7 +68,7 @@ struct SortBuffers {
     long long tiles;                    // tiles at capacity
     long long groups;                   // tile groups at capacity
 };
-constexpr int kSortGroup = 16;          // tiles per group of the pass's prefix
+constexpr int kSortGroup = 32;          // tiles per group of the pass's prefix
 
 struct BigQuad {            // a quad rasterized by the exact tile emulation
     int px[4], py[4];
@@ -112,7 +112,11 @@ long long sort_tiles(long long n);
 // Launches the radix passes of digits [0, n_passes) (a pass whose digit is
 // the same for every key of the frame returns at once).
 void launch_canonical_sort(const int* root_prefix, const SubPatches& in, const SubPatches& out, const SortBuffers& sb,
-                           unsigned long long* ctrl, long long spin_limit, int n_passes, cudaStream_t s);
+                           unsigned long long* ctrl, long long spin_limit, int n_passes, int resident_grid,
+                           cudaStream_t s);
+// Blocks of the sort's pass kernel resident at once (also sets its shared
+// memory size; call outside stream capture).
+int canonical_sort_grid();
 // The radix passes the keys of a frame can need: root bits up to `roots`
 // above at most min(32, max_split_depth + 1) path bits.
 int canonical_sort_passes(int max_split_depth, long long roots);

@@ -16,19 +16,23 @@
 // The sort is a least-significant-digit radix sort over 8-bit digits of a
 // key that packs the root above the frame's D path bits (D = the deepest
 // emitted sub-patch, which bound-and-split records; below bit 32 - D every
-// path is zero, so the order is that of (root << 32 | path)).  Digit counts
+// path is zero, so the order is that of (root << 32 | path)).  Keys are 32
+// bits wide when the frame's root and path bits fit, else 64.  Digit counts
 // of every pass are taken once, up front (Adinets & Merrill's one-sweep
-// radix sort).  A pass splits the keys into tiles, one per resident block
-// at a time (rounds of gridDim.x tiles): each tile ranks its digits stably
-// (per-warp counters; lanes with equal digits found by one ballot per digit
-// bit), publishes its digit counts, waits until every tile of its round and
+// radix sort).  A pass splits the keys into tiles of kSortTile, one per
+// resident block at a time (rounds of gridDim.x tiles): each tile ranks its
+// digits stably (per-warp counters; lanes with equal digits found by one
+// ballot per digit bit), publishes its digit counts, reorders itself by
+// digit in shared memory while it waits until every tile of its round and
 // the earlier ones has published, adds up the counts of the tiles before it
-// (independent loads, no chain of waits), and scatters.  The last pass that
-// moves keys writes the sub-patch records themselves in canonical order.
-//   keys  -- keys, identity source slots, digit counts of every pass;
+// (independent loads, no chain of waits), and writes each digit's run of
+// the tile to consecutive addresses.  The first pass that moves keys forms
+// them from the records; the last writes the sub-patch records themselves
+// in canonical order.
+//   keys  -- digit counts of every pass;
 //   pass  -- one launch per digit position the frame's keys can have; a pass
 //            whose digit is the same for every key returns at once.
-// Every wait is bounded (MP_ERR_TIMEOUT, no scatter after it).
+// Every wait is bounded (MP_ERR_TIMEOUT, no write after it).
 #include "mp_bns_loop.cuh"
 
 namespace mp {
@@ -38,7 +42,7 @@ namespace {
 constexpr int kKeysBlock = 1024;
 constexpr int kSortBlock = 512;
 constexpr int kSortWarps = kSortBlock / 32;
-constexpr int kSortItems = 16;
+constexpr int kSortItems = 8;
 constexpr int kSortTile = kSortBlock * kSortItems;   // keys per tile
 constexpr int kDigits = 256;
 
@@ -60,7 +64,8 @@ __device__ __forceinline__ unsigned* hist_of(const SortBuffers& sb, unsigned epo
     return sb.hist + (epoch & 1u) * kSortPasses * kDigits;
 }
 
-__device__ __forceinline__ unsigned digit_of(unsigned long long key, int pass) {
+template <typename K>
+__device__ __forceinline__ unsigned digit_of(K key, int pass) {
     return (unsigned)(key >> (8 * pass)) & 0xffu;
 }
 
@@ -93,10 +98,10 @@ __device__ __forceinline__ int key_bits(const unsigned long long* ctrl, unsigned
     return root_bits + (int)D;
 }
 
-// Keys, identity source slots, and the digit counts of the passes the keys
-// reach (warp-aggregated: one shared add per distinct digit of a warp's 32
-// keys); clears the next frame's counts, this frame's tile-group counts and
-// its published-tile counters.
+// Digit counts of the passes the frame's keys reach (warp-aggregated: one
+// shared add per distinct digit of a warp's 32 keys); clears the next
+// frame's counts, this frame's tile-group counts and its published-tile
+// counters.
 __global__ void __launch_bounds__(kKeysBlock) sort_keys_kernel(const int* __restrict__ root_prefix, SubPatches in,
                                                                SortBuffers sb, unsigned long long* ctrl,
                                                                int n_passes) {
@@ -122,10 +127,7 @@ __global__ void __launch_bounds__(kKeysBlock) sort_keys_kernel(const int* __rest
         unsigned long long key = 0;
         if (valid) {
             const int2 m = in.meta[i];
-            const unsigned root = (unsigned)(__ldg(root_prefix + m.y) + m.x);
-            key = pack_key(root, in.path[i], D);
-            sb.keys[0][i] = key;
-            sb.vals[0][i] = (unsigned)i;
+            key = pack_key((unsigned)(__ldg(root_prefix + m.y) + m.x), in.path[i], D);
         }
         for (int p = 0; p < active; ++p) {
             const unsigned d = digit_of(key, p);
@@ -141,32 +143,227 @@ __global__ void __launch_bounds__(kKeysBlock) sort_keys_kernel(const int* __rest
     }
 }
 
+// Shared memory of one pass block (the 64-bit layout; 32-bit keys use the
+// front half of `keys`).
+struct PassSmem {
+    unsigned long long keys[kSortTile];           // the tile in digit order
+    unsigned vals[kSortTile];
+    unsigned short wcount[kSortWarps][kDigits];   // per warp digit counts, then offsets in the tile's digit run
+    unsigned tstart[kDigits];                     // exclusive digit starts within the tile
+    unsigned start[kDigits];                      // exclusive digit starts of the pass
+    unsigned base[kDigits];                       // global position of the tile's first key of each digit
+    unsigned part[kDigits];                       // the earlier tiles of the tile's own group, per digit
+    unsigned warp_sum[kSortWarps];
+    int fail;
+};
+
+// Exclusive prefix over the 256 values that threads 0-255 hold (every
+// thread of the block calls it; ends with a barrier).
+__device__ __forceinline__ unsigned scan_digits(unsigned v, unsigned* warp_sum) {
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    unsigned x = v;
+    if (tid < kDigits) {
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) warp_sum[warp] = x;
+    }
+    __syncthreads();
+    unsigned before = 0;
+    if (tid < kDigits)
+        for (int w = 0; w < warp; ++w) before += warp_sum[w];
+    __syncthreads();
+    return before + x - v;
+}
+
+// One moving pass over keys of type K (see sort_pass_kernel).
+//   from_records -- the first moving pass: keys formed from the records
+//   last         -- the last moving pass: records written in key order
+template <typename K>
+__device__ __forceinline__ void pass_body(PassSmem& sm, const int* __restrict__ root_prefix, const SubPatches& in,
+                                          const SubPatches& out, const SortBuffers& sb, unsigned long long* ctrl,
+                                          int pass, long long n, unsigned D, int moves_before, bool last,
+                                          unsigned h_pass, long long spin_limit) {
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const bool from_records = moves_before == 0;
+    // (selects, not an indexed load: the parameter arrays stay in registers)
+    const int src = (moves_before - 1) & 1, dst_buf = moves_before & 1;
+    const K* __restrict__ kin = reinterpret_cast<const K*>(src ? sb.keys[1] : sb.keys[0]);
+    const unsigned* __restrict__ vin = src ? sb.vals[1] : sb.vals[0];
+    K* kout = reinterpret_cast<K*>(dst_buf ? sb.keys[1] : sb.keys[0]);
+    unsigned* vout = dst_buf ? sb.vals[1] : sb.vals[0];
+    K* skeys = reinterpret_cast<K*>(sm.keys);
+    unsigned* groups = sb.group_counts + (long long)pass * sb.groups * kDigits;
+    unsigned long long* published = ctrl + (kSortTicket + pass) * kCtrlStride;
+    {
+        const unsigned st = scan_digits(tid < kDigits ? h_pass : 0u, sm.warp_sum);
+        if (tid < kDigits) sm.start[tid] = st;
+        if (tid == 0) sm.fail = 0;
+    }
+    const long long n_tiles = (n + kSortTile - 1) / kSortTile;
+    const unsigned lt = (1u << lane) - 1u;
+    for (long long tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
+        const long long t0 = tile * kSortTile;
+        const int tn = (int)(n - t0 < kSortTile ? n - t0 : kSortTile);
+        for (int i = tid; i < kSortWarps * kDigits; i += kSortBlock) (&sm.wcount[0][0])[i] = 0;
+        __syncthreads();
+        // warp w ranks the keys [t0 + w * 32 * kSortItems, + 32 * kSortItems):
+        // item i of lane l is key i * 32 + l of that run, so the ranks follow key order
+        const long long run = t0 + (long long)warp * 32 * kSortItems;
+        K k[kSortItems];
+        unsigned v[kSortItems];
+#pragma unroll
+        for (int i = 0; i < kSortItems; ++i) {
+            const long long idx = run + i * 32 + lane;
+            k[i] = 0;
+            v[i] = 0;
+            if (idx < n) {
+                if (from_records) {
+                    const int2 m = __ldcg(in.meta + idx);
+                    k[i] = (K)pack_key((unsigned)(__ldg(root_prefix + m.y) + m.x), __ldcg(in.path + idx), D);
+                    v[i] = (unsigned)idx;
+                } else {
+                    k[i] = __ldcg(kin + idx);
+                    v[i] = __ldcg(vin + idx);
+                }
+            }
+        }
+        unsigned short* wc = sm.wcount[warp];
+        unsigned rank[kSortItems];
+#pragma unroll
+        for (int i = 0; i < kSortItems; ++i) {
+            const bool valid = run + i * 32 + lane < n;
+            const unsigned d = digit_of(k[i], pass);
+            const unsigned peers = match_digit(d, valid);
+            const unsigned before = valid ? wc[d] : 0u;
+            rank[i] = before + (unsigned)__popc(peers & lt);
+            __syncwarp();
+            if (valid && (peers & lt) == 0) wc[d] = (unsigned short)(before + (unsigned)__popc(peers));
+            __syncwarp();
+        }
+        __syncthreads();
+        // thread d: the warps' offsets within digit d's run of the tile, the
+        // tile's count of d (published), and the tile's digit starts
+        unsigned tot = 0;
+        if (tid < kDigits) {
+#pragma unroll
+            for (int w = 0; w < kSortWarps; ++w) {
+                const unsigned c = sm.wcount[w][tid];
+                sm.wcount[w][tid] = (unsigned short)tot;
+                tot += c;
+            }
+            sb.counts[tile * kDigits + tid] = tot;
+            if (tot) atomicAdd(groups + (tile / kSortGroup) * kDigits + tid, tot);
+            __threadfence();
+        }
+        const unsigned ts = scan_digits(tot, sm.warp_sum);
+        if (tid == 0) {
+            // publish (every count above is fenced before the barrier in scan_digits)
+            __threadfence();
+            atomicAdd(published, 1ull);
+        }
+        if (tid < kDigits) sm.tstart[tid] = ts;
+        __syncthreads();
+        // the tile in digit order, in shared memory
+#pragma unroll
+        for (int i = 0; i < kSortItems; ++i) {
+            if (run + i * 32 + lane < n) {
+                const unsigned d = digit_of(k[i], pass);
+                const unsigned local = sm.tstart[d] + sm.wcount[warp][d] + rank[i];
+                skeys[local] = k[i];
+                sm.vals[local] = v[i];
+            }
+        }
+        if (tid == 0) {
+            // wait until every tile up to the end of this round has published
+            const long long round_end = (tile / gridDim.x + 1) * gridDim.x;
+            const unsigned long long need = (unsigned long long)(round_end < n_tiles ? round_end : n_tiles);
+            long long spins = 0;
+            while (ld_acquire_u64(published) < need) {
+                if (++spins > spin_limit) {
+                    sm.fail = 1;
+                    break;
+                }
+                __nanosleep(64);
+            }
+            __threadfence();
+        }
+        __syncthreads();
+        if (sm.fail) {
+            // a wait ran out: report it and write nothing with a wrong base
+            if (tid == 0) set_status(ctrl, kErrTimeout);
+            return;
+        }
+        {
+            // counts of the earlier tiles, digit d: thread d adds the whole
+            // groups before this tile's group, thread d + 256 the earlier
+            // tiles of its own group
+            const int d = tid & (kDigits - 1);
+            const long long g = tile / kSortGroup;
+            unsigned sum = 0;
+            if (tid < kDigits) {
+                for (long long j = 0; j < g; j += 16) {
+                    unsigned x[16];
+#pragma unroll
+                    for (int u = 0; u < 16; ++u) x[u] = j + u < g ? __ldcg(groups + (j + u) * kDigits + d) : 0u;
+#pragma unroll
+                    for (int u = 0; u < 16; ++u) sum += x[u];
+                }
+            } else {
+                for (long long j = g * kSortGroup; j < tile; j += 16) {
+                    unsigned x[16];
+#pragma unroll
+                    for (int u = 0; u < 16; ++u) x[u] = j + u < tile ? __ldcg(sb.counts + (j + u) * kDigits + d) : 0u;
+#pragma unroll
+                    for (int u = 0; u < 16; ++u) sum += x[u];
+                }
+                sm.part[d] = sum;
+            }
+            __syncthreads();
+            if (tid < kDigits) sm.base[d] = sm.start[d] + sum + sm.part[d];
+            __syncthreads();
+        }
+        // each digit's run of the tile to consecutive addresses
+        for (int j = tid; j < tn; j += kSortBlock) {
+            const K key = skeys[j];
+            const unsigned d = digit_of(key, pass);
+            const long long dst = (long long)sm.base[d] + (j - (int)sm.tstart[d]);
+            if (dst < n) {
+                const unsigned sv = sm.vals[j];
+                if (last) {
+                    if (dst < out.capacity && sv < (unsigned)n) {
+                        out.range[dst] = __ldcg(in.range + sv);
+                        out.meta[dst] = __ldcg(in.meta + sv);
+                    }
+                } else {
+                    kout[dst] = key;
+                    vout[dst] = sv;
+                }
+            }
+        }
+        __syncthreads();
+    }
+}
+
 // One radix pass.  Tile t (kSortTile keys) is block t % gridDim.x's, in
 // round t / gridDim.x; the grid is resident, and every block publishes its
 // tile's digit counts before it waits, so the waits end.  A tile's start in
 // digit bin d is the bin's start plus the counts of the earlier tiles, read
 // as the sums of whole groups of kSortGroup tiles (accumulated as tiles
-// publish) and the single counts of its own group's earlier tiles.  Warp w
-// of a tile owns the keys [tile * kSortTile + w * 32 * kSortItems, +32 *
-// kSortItems); item i of lane l is key i * 32 + l of that run, so a warp
-// ranks its run in key order and the pass is stable.  The last pass that
-// moves keys writes the records of `in` to `out` in their sorted order
-// instead of the keys.
-__global__ void __launch_bounds__(kSortBlock) sort_pass_kernel(SubPatches in, SubPatches out, SortBuffers sb,
-                                                               unsigned long long* ctrl, int pass, int n_passes,
-                                                               long long spin_limit) {
-    __shared__ unsigned s_wcount[kSortWarps][kDigits];   // per warp digit counts, then exclusive offsets
-    __shared__ unsigned s_start[kDigits];                // the pass's exclusive digit starts
-    __shared__ unsigned s_base[kDigits];                 // global start of each digit's run of this tile
-    __shared__ unsigned s_part[kDigits];                 // half of the earlier tiles' counts
-    __shared__ unsigned s_warp[kSortWarps];
-    __shared__ unsigned short s_rank[kSortItems][kSortBlock];   // rank of each item within its warp's run
-    __shared__ int s_fail;
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+// publish) and the single counts of its own group's earlier tiles.
+__global__ void __launch_bounds__(kSortBlock, 2) sort_pass_kernel(const int* __restrict__ root_prefix, SubPatches in,
+                                                                  SubPatches out, SortBuffers sb,
+                                                                  unsigned long long* ctrl, int pass, int n_passes,
+                                                                  long long spin_limit) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    PassSmem& sm = *reinterpret_cast<PassSmem*>(smem_raw);
+    const int tid = threadIdx.x;
     const long long n = sort_count(ctrl, in, sb);
-    const unsigned epoch = frame_epoch(ctrl);
-    const unsigned* hist = hist_of(sb, epoch);
-    const int bits = key_bits(ctrl, nullptr);
+    const unsigned* hist = hist_of(sb, frame_epoch(ctrl));
+    unsigned D = 0;
+    const int bits = key_bits(ctrl, &D);
     const int active = (bits + 7) / 8 < n_passes ? (bits + 7) / 8 : n_passes;
     // passes that move keys: those within the keys' bits whose digit is not
     // the same for every key (the counts of all passes are loaded first)
@@ -175,10 +372,12 @@ __global__ void __launch_bounds__(kSortBlock) sort_pass_kernel(SubPatches in, Su
     for (int q = 0; q < kSortPasses; ++q) h[q] = q < active && tid < kDigits ? hist[q * kDigits + tid] : 0u;
     int moves_before = 0, moves_after = 0;
     bool moves = false;
+    unsigned h_pass = 0;
 #pragma unroll
     for (int q = 0; q < kSortPasses; ++q) {
         if (q >= active) break;
         const int same = __syncthreads_or(tid < kDigits && (long long)h[q] == n);
+        if (q == pass) h_pass = h[q];
         if (!same) {
             if (q < pass) ++moves_before;
             else if (q == pass) moves = true;
@@ -196,146 +395,11 @@ __global__ void __launch_bounds__(kSortBlock) sort_pass_kernel(SubPatches in, Su
         return;
     }
     const bool last = moves_after == 0;
-    const int src = moves_before & 1;
-    // (selects, not an indexed load: the parameter arrays stay in registers)
-    const unsigned long long* __restrict__ kin = src ? sb.keys[1] : sb.keys[0];
-    const unsigned* __restrict__ vin = src ? sb.vals[1] : sb.vals[0];
-    unsigned long long* kout = src ? sb.keys[0] : sb.keys[1];
-    unsigned* vout = src ? sb.vals[0] : sb.vals[1];
-    unsigned* groups = sb.group_counts + (long long)pass * sb.groups * kDigits;
-    unsigned long long* published = ctrl + (kSortTicket + pass) * kCtrlStride;
-    if (tid < kDigits) {
-        // exclusive digit starts of this pass (warps 0-7)
-        const unsigned c = h[pass];
-        unsigned x = c;
-        for (int o = 1; o < 32; o <<= 1) {
-            const unsigned y = __shfl_up_sync(0xffffffffu, x, o);
-            if (lane >= o) x += y;
-        }
-        if (lane == 31) s_warp[warp] = x;
-        s_start[tid] = x - c;
-    }
-    if (tid == 0) s_fail = 0;
-    __syncthreads();
-    if (tid < kDigits) {
-        unsigned before = 0;
-        for (int w = 0; w < warp; ++w) before += s_warp[w];
-        s_start[tid] += before;
-    }
-    const long long n_tiles = (n + kSortTile - 1) / kSortTile;
-    const unsigned lt = (1u << lane) - 1u;
-    for (long long tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
-        for (int i = tid; i < kSortWarps * kDigits; i += kSortBlock) (&s_wcount[0][0])[i] = 0;
-        __syncthreads();
-        const long long run = tile * kSortTile + (long long)warp * 32 * kSortItems;
-        unsigned long long k[kSortItems];
-        unsigned v[kSortItems];
-#pragma unroll
-        for (int i = 0; i < kSortItems; ++i) {
-            const long long idx = run + i * 32 + lane;
-            k[i] = idx < n ? __ldcg(kin + idx) : 0ull;
-            v[i] = idx < n ? __ldcg(vin + idx) : 0u;
-        }
-        unsigned* wc = s_wcount[warp];
-#pragma unroll
-        for (int i = 0; i < kSortItems; ++i) {
-            const bool valid = run + i * 32 + lane < n;
-            const unsigned d = digit_of(k[i], pass);
-            const unsigned peers = match_digit(d, valid);
-            const unsigned before = valid ? wc[d] : 0u;
-            s_rank[i][tid] = (unsigned short)(before + (unsigned)__popc(peers & lt));
-            __syncwarp();
-            if (valid && (peers & lt) == 0) wc[d] = before + (unsigned)__popc(peers);
-            __syncwarp();
-        }
-        __syncthreads();
-        if (tid < kDigits) {
-            // thread d: warp offsets within the tile and the tile's count, published
-            const int d = tid;
-            unsigned tot = 0;
-#pragma unroll
-            for (int w = 0; w < kSortWarps; ++w) {
-                const unsigned c = s_wcount[w][d];
-                s_wcount[w][d] = tot;
-                tot += c;
-            }
-            sb.counts[tile * kDigits + d] = tot;
-            if (tot) atomicAdd(groups + (tile / kSortGroup) * kDigits + d, tot);
-        }
-        __syncthreads();
-        if (tid == 0) {
-            // publish, then wait until every tile up to the end of this round has
-            __threadfence();
-            atomicAdd(published, 1ull);
-            const long long round_end = (tile / gridDim.x + 1) * gridDim.x;
-            const unsigned long long need = (unsigned long long)(round_end < n_tiles ? round_end : n_tiles);
-            long long spins = 0;
-            while (ld_acquire_u64(published) < need) {
-                if (++spins > spin_limit) {
-                    s_fail = 1;
-                    break;
-                }
-                __nanosleep(64);
-            }
-            __threadfence();
-        }
-        __syncthreads();
-        if (s_fail) {
-            // a wait ran out: report it and write nothing with a wrong base
-            if (tid == 0) set_status(ctrl, kErrTimeout);
-            return;
-        }
-        {
-            // counts of the earlier tiles, digit d: thread d adds the whole
-            // groups before this tile's group, thread d + 256 the earlier
-            // tiles of its own group
-            const int d = tid & (kDigits - 1);
-            const long long g = tile / kSortGroup;
-            unsigned sum = 0;
-            if (tid < kDigits) {
-                long long j = 0;
-                for (; j + 8 <= g; j += 8) {
-                    unsigned x[8];
-#pragma unroll
-                    for (int u = 0; u < 8; ++u) x[u] = __ldcg(groups + (j + u) * kDigits + d);
-#pragma unroll
-                    for (int u = 0; u < 8; ++u) sum += x[u];
-                }
-                for (; j < g; ++j) sum += __ldcg(groups + j * kDigits + d);
-            } else {
-                unsigned x[kSortGroup];
-#pragma unroll
-                for (int u = 0; u < kSortGroup; ++u)
-                    x[u] = g * kSortGroup + u < tile ? __ldcg(sb.counts + (g * kSortGroup + u) * kDigits + d) : 0u;
-#pragma unroll
-                for (int u = 0; u < kSortGroup; ++u) sum += x[u];
-                s_part[d] = sum;
-            }
-            __syncthreads();
-            if (tid < kDigits) s_base[d] = s_start[d] + sum + s_part[d];
-            __syncthreads();
-        }
-#pragma unroll
-        for (int i = 0; i < kSortItems; ++i) {
-            const long long idx = run + i * 32 + lane;
-            if (idx < n) {
-                const unsigned dg = digit_of(k[i], pass);
-                const long long dst = (long long)s_base[dg] + s_wcount[warp][dg] + s_rank[i][tid];
-                if (dst < n) {
-                    if (last) {
-                        if (dst < out.capacity && v[i] < (unsigned)n) {
-                            out.range[dst] = __ldcg(in.range + v[i]);
-                            out.meta[dst] = __ldcg(in.meta + v[i]);
-                        }
-                    } else {
-                        kout[dst] = k[i];
-                        vout[dst] = v[i];
-                    }
-                }
-            }
-        }
-        __syncthreads();
-    }
+    if (bits <= 32)
+        pass_body<unsigned>(sm, root_prefix, in, out, sb, ctrl, pass, n, D, moves_before, last, h_pass, spin_limit);
+    else
+        pass_body<unsigned long long>(sm, root_prefix, in, out, sb, ctrl, pass, n, D, moves_before, last, h_pass,
+                                      spin_limit);
 }
 
 int sm_count() {
@@ -343,17 +407,6 @@ int sm_count() {
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     return sms;
-}
-
-// Blocks resident at once (the pass's waits rely on it).
-int pass_grid() {
-    static int grid = 0;
-    if (grid == 0) {
-        int per_sm = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sort_pass_kernel, kSortBlock, 0);
-        grid = sm_count() * (per_sm < 1 ? 1 : per_sm);
-    }
-    return grid;
 }
 
 }  // namespace
@@ -369,13 +422,23 @@ int canonical_sort_passes(int max_split_depth, long long roots) {
     return bits <= 8 ? 1 : (bits + 7) / 8;
 }
 
+int canonical_sort_grid() {
+    // blocks resident at once (the passes' waits rely on it)
+    cudaFuncSetAttribute(sort_pass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(PassSmem));
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sort_pass_kernel, kSortBlock, sizeof(PassSmem));
+    return sm_count() * (per_sm < 1 ? 1 : per_sm);
+}
+
 void launch_canonical_sort(const int* root_prefix, const SubPatches& in, const SubPatches& out, const SortBuffers& sb,
-                           unsigned long long* ctrl, long long spin_limit, int n_passes, cudaStream_t s) {
+                           unsigned long long* ctrl, long long spin_limit, int n_passes, int resident_grid,
+                           cudaStream_t s) {
     sort_keys_kernel<<<sm_count(), kKeysBlock, 0, s>>>(root_prefix, in, sb, ctrl, n_passes);
     const long long tiles = sb.tiles < 1 ? 1 : sb.tiles;
-    const int grid = (int)(tiles < pass_grid() ? tiles : pass_grid());
+    const int grid = (int)(tiles < resident_grid ? tiles : resident_grid);
     for (int p = 0; p < n_passes; ++p)
-        sort_pass_kernel<<<grid, kSortBlock, 0, s>>>(in, out, sb, ctrl, p, n_passes, spin_limit);
+        sort_pass_kernel<<<grid, kSortBlock, sizeof(PassSmem), s>>>(root_prefix, in, out, sb, ctrl, p, n_passes,
+                                                                    spin_limit);
 }
 
 }  // namespace mp
