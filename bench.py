@@ -36,18 +36,40 @@ WORKLOAD = "mixed4096_1920x1080"
 METRIC = "micropolygons/s (batched path, 4096-patch mixed Bezier/Gregory scene, 1920x1080)"
 L2_FLUSH_BYTES = 256 << 20
 
-# DRAM bytes (read + write) per launch of each stage's kernel on this
-# workload, from one ncu capture each (dram__bytes_read.sum +
-# dram__bytes_write.sum; profiles/raster_fused_mixed4096_1920x1080.md,
-# profiles/bns_persistent_mixed4096_1920x1080.md and
-# profiles/resolve_mixed4096_1920x1080.md).  ncu replays with cold
-# caches, so these are upper bounds for a launch inside a frame.
-NCU_TRAFFIC = {"dice_raster": 101_992_192 + 65_780_480, "bound_split": 2_698_240 + 200_370_944,
-               "resolve_or_shade": 62_738_688 + 8_585_472}
-# Warp instructions per launch (smsp__inst_executed.sum) from the same
-# captures: the dice+raster kernel is bound by instruction issue, whose peak
-# is 4 warp instructions per SM per cycle.
-NCU_INST = {"dice_raster": 1_068_466_194, "bound_split": 161_999_590}
+# DRAM bytes (read + write) and warp instructions per launch of each stage's
+# kernel on this workload, from one ncu capture each (dram__bytes_read.sum +
+# dram__bytes_write.sum, smsp__inst_executed.sum; the summaries under
+# profiles/), with a hash of the sources the kernel was built from at the
+# capture.  A figure whose hash no longer matches the sources describes an
+# older kernel and is left out of the bench line.  ncu replays with cold
+# caches, so the traffic is an upper bound for a launch inside a frame.
+CSRC = os.path.join(ROOT, "micropolis_gb300", "csrc")
+KERNEL_SOURCES = {
+    "dice_raster": ["mp_raster.cu", "mp_device.cuh", "mp_bns_loop.cuh", "mp_internal.h"],
+    "bound_split": ["mp_bns.cu", "mp_device.cuh", "mp_bns_loop.cuh", "mp_internal.h"],
+    "resolve_or_shade": ["mp_raster.cu", "mp_device.cuh", "mp_bns_loop.cuh", "mp_internal.h"],
+    "canonical_sort_or_sample": ["mp_sort.cu", "mp_bns_loop.cuh", "mp_internal.h"],
+}
+NCU_FIGURES = {}
+
+
+def source_hash(stage: str) -> str:
+    """SHA-256 (first 16 hex digits) of the sources a stage's kernel is built from."""
+    import hashlib
+    h = hashlib.sha256()
+    for f in KERNEL_SOURCES.get(stage, []):
+        with open(os.path.join(CSRC, f), "rb") as fh:
+            h.update(fh.read())
+    return h.hexdigest()[:16]
+
+
+def ncu_figure(stage: str, key: str):
+    """The captured figure `key` ("traffic" or "inst") of a stage's kernel,
+    or None when there is none for the current sources."""
+    fig = NCU_FIGURES.get(stage)
+    if not fig or fig.get("source") != source_hash(stage):
+        return None
+    return fig.get(key)
 
 
 def parse():
@@ -153,50 +175,86 @@ def measured_peaks():
 # --------------------------------------------------------------------------
 # CPU baseline (the oracle's restatement of the reference CPU path)
 
+CPU_CHUNKS = 128        # a frame's patches in this many strided chunks, dealt to the cores as they free up
+_SCENES = {}
+
+
 def _cpu_chunk(args):
-    """Render a bounded sample (patch subset) of the workload on one core."""
-    name, draw_slices = args
+    """Render one chunk of a frame (every `stride`-th patch of each draw from
+    `first`) on one core: bound-and-split, dice, shade and sample.  Returns
+    (micropolygons, seconds)."""
+    name, first, stride = args
     sys.path.insert(0, ROOT)
     from micropolis_gb300 import scenes
     from oracle import oracle
-    sc = scenes.WORKLOADS[name]()
-    for d, sl in zip(sc.draws, draw_slices):
-        # (first, end) patch range, or (first, end, stride) for an interleaved share
-        d.mesh = scenes.Mesh(d.mesh.type, d.mesh.cp[slice(*sl)])
+    if name not in _SCENES:
+        _SCENES[name] = scenes.WORKLOADS[name]()
+    full = _SCENES[name]
+    sc = scenes.Scene(full.name, full.width, full.height,
+                      [scenes.Draw(scenes.Mesh(d.mesh.type, d.mesh.cp[first::stride]), d.mv, d.color, d.view)
+                       for d in full.draws], fovy=full.fovy, near=full.near, options=full.options)
     t = time.perf_counter()
     _, _, st = oracle.render(sc)
     return st["micropolygons"], time.perf_counter() - t
 
 
-def cpu_baseline(name: str, procs: int, patches_per_proc: int, pool=None):
-    """micropolygons/s of the oracle path on `procs` processes, each rendering
-    its own slice of every draw's patches (a bounded sample); with
-    patches_per_proc = 0 the processes share one frame (process p renders
-    every procs-th patch of every draw, starting at patch p).  Returns (rate,
-    micropolygons, wall s, busiest process s)."""
-    from micropolis_gb300 import scenes
-    sc = scenes.WORKLOADS[name]()
-    jobs = []
-    for p in range(procs):
-        sl = []
-        for d in sc.draws:
-            n = d.mesh.n_patches
-            if patches_per_proc <= 0:
-                sl.append((p, n, procs))    # every procs-th patch: the shares cost about the same
-                continue
-            share = max(1, patches_per_proc // len(sc.draws))
-            a = (p * share) % max(1, n)
-            sl.append((a, min(a + share, n)))
-        jobs.append((name, sl))
+def cpu_frame(name: str, pool, chunks: int = CPU_CHUNKS):
+    """One frame of workload `name` on the CPU: its patches in `chunks`
+    strided chunks (chunk c = every chunks-th patch of each draw from patch
+    c), dealt to the pool's processes as they free up, so that the
+    heavy-tailed cost per patch does not leave cores idle.  Returns
+    (micropolygons/s = the frame's micropolygons / wall time, micropolygons,
+    wall s)."""
     t = time.perf_counter()
-    if pool is None:
-        res = [_cpu_chunk(j) for j in jobs]
-    else:
-        res = pool.map(_cpu_chunk, jobs)
+    res = list(pool.imap_unordered(_cpu_chunk, [(name, c, chunks) for c in range(chunks)]))
     wall = time.perf_counter() - t
     mpoly = sum(r[0] for r in res)
-    busy = max(r[1] for r in res)
-    return mpoly / busy, mpoly, wall, busy
+    return mpoly / wall, mpoly, wall
+
+
+def cpu_model() -> str:
+    """The host CPU's model name (lscpu; /proc/cpuinfo as a fallback)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.strip().startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    import platform
+    return platform.machine()
+
+
+def cpu_baseline_line(name: str, pool, cores: int, frames: int, warmup: int = 1):
+    """The CPU baseline of one workload: `warmup` untimed frames, then the
+    best of `frames` timed ones (cpu_frame), with how it was measured."""
+    for _ in range(warmup):
+        cpu_frame(name, pool)
+    runs = [cpu_frame(name, pool) for _ in range(frames)]
+    best = max(runs, key=lambda r: r[0])
+    return {"value": best[0], "unit": "micropolygons/s", "cores": cores, "kind": "port", "cpu_model": cpu_model(),
+            "sample": f"one whole frame of {name} per sample: bound&split+dice+shade+sample of its patches in "
+                      f"{CPU_CHUNKS} strided chunks dealt to {cores} processes as they free up; best of {frames} "
+                      f"after {warmup} warm-up ({best[1]} micropolygons in {best[2]:.2f} s)",
+            "frames_s": [round(r[2], 3) for r in runs]}
+
+
+def plain_grid_bytes(PS: int, subpatches: int, ms: float) -> dict:
+    """Grid traffic of the plain per-pass path, which keeps the reference's
+    grids in device memory (src/Reyes/RendererCL.cpp:32-48): per sub-patch
+    (PS+1)^2 vertices of float4 position + int2 pixel + float depth, PS^2
+    float4 quad colours and (PS/8)^2 int4 block bounds, each written once and
+    read once."""
+    per = (PS + 1) ** 2 * 28 + PS * PS * 16 + (PS // 8) ** 2 * 16
+    total = 2 * per * subpatches
+    return {"grid_bytes_per_subpatch": per, "grid_bytes_per_frame": total,
+            "grid_gbs": total / (ms / 1e3) / 1e9 if ms > 0 else None}
 
 
 def cpu_pool(procs: int):
@@ -213,26 +271,24 @@ def run_reference(args):
     if rank != 0:
         return 0
     cores = os.cpu_count() or 1
-    # one step = one whole frame's 4096 patches shared over the cores
-    # (process p takes every cores-th patch of each draw)
-    per = 0
+    # one step = one whole frame, rendered by all cores (cpu_frame)
     vals = []
     with cpu_pool(cores) as pool:
-        pool.map(_cpu_chunk, [(WORKLOAD, [(0, 1), (0, 1)])] * cores)   # import and build in every worker
+        pool.map(_cpu_chunk, [(WORKLOAD, 0, 4096)] * cores)   # import, build and make the scene in every worker
         for i in range(args.warmup + args.steps):
-            v, mpoly, wall, busy = cpu_baseline(WORKLOAD, cores, per, pool)
+            v, mpoly, wall = cpu_frame(WORKLOAD, pool)
             if i >= args.warmup:
-                vals.append((v, mpoly, busy))
+                vals.append((v, mpoly, wall))
     value = sum(v[1] for v in vals) / sum(v[2] for v in vals)
+    sample = (f"one whole frame per step: bound&split+dice+shade+sample of its 4096 patches in {CPU_CHUNKS} "
+              f"strided chunks dealt to {cores} processes as they free up")
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "micropolygons/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(v[2] for v in vals),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded generator, no dataset)",
-            "config": {"workload": WORKLOAD, "sample": f"one frame per step over {cores} processes"},
+            "config": {"workload": WORKLOAD, "sample": sample},
             "cpu_baseline": {"value": value, "unit": "micropolygons/s", "cores": cores, "kind": "port",
-                             "sample": f"one frame per step: {cores} processes, each bound&split+dice+shade+sample "
-                                       f"of every {cores}-th of the 4096 patches; bound&split single-threaded per "
-                                       f"process"},
+                             "cpu_model": cpu_model(), "sample": sample},
             "e2e": {"value": value, "unit": "micropolygons/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
     return 0
@@ -251,7 +307,7 @@ def all_configs(args):
     peak_gbs, peak_kind = measured_peaks()
     cores = os.cpu_count() or 1
     pool = cpu_pool(cores)
-    pool.map(_cpu_chunk, [("heightfield_1024x768", [(0, 1)])] * cores)
+    pool.map(_cpu_chunk, [("heightfield_1024x768", 0, 64)] * cores)
     atom_peak = None
     for name, make in scenes.WORKLOADS.items():
         if args.workload and name not in args.workload:
@@ -282,6 +338,9 @@ def all_configs(args):
             cp_alg = sum(d.mesh.n_patches * d.mesh.cp.shape[1] * 12 for d in sc.draws)
             views = line["views"]
             frame_bytes = cp_alg + st["subpatches"] * 20 + views * sc.width * sc.height * (8 + 8 + 16)
+            if path == "plain":
+                line["plain_grids"] = plain_grid_bytes(int(sc.options.get("reyes_patch_size", 8)),
+                                                       st["subpatches"], m)
             line[path] = {"ms_per_frame": m, "micropolygons": st["micropolygons"],
                           "value": st["micropolygons"] / (m / 1e3), "subpatches": st["subpatches"],
                           "fragments": st["fragments"], "passes": st["passes"], "kernels": st["kernels"],
@@ -289,10 +348,7 @@ def all_configs(args):
                           "frac_atomic": st["fragments"] / (m / 1e3) / atom_peak}
             r.close()
         line["batched_over_plain"] = line["batched"]["value"] / line["plain"]["value"]
-        cv, cmp, cwall, cbusy = cpu_baseline(name, cores, 0, pool)
-        line["cpu_baseline"] = {"value": cv, "unit": "micropolygons/s", "cores": cores, "kind": "port",
-                                "sample": f"one frame shared over {cores} processes ({cmp} micropolygons, "
-                                          f"busiest process {cbusy:.2f} s)"}
+        line["cpu_baseline"] = cpu_baseline_line(name, pool, cores, frames=3 if sc.n_patches > 10000 else 5)
         if sc.options.get("displacement"):
             line["adjoint"] = adjoint.bench_bwd_fwd(stream, workload=name, steps=5)
         line["peaks"] = {"hbm_gbs": peak_gbs, "hbm_kind": peak_kind, "atomic_per_s": atom_peak}
@@ -309,9 +365,16 @@ def views64_leg(stream):
     from micropolis_gb300 import autotune, scenes
     from micropolis_gb300.renderer import render_scene, renderer_for
     sc = scenes.views64_512x512()
-    best = autotune.tune(sc, frames=3, warmup=1, use_cache=False)
-    out = {"patches": sc.n_patches, "views": 64, "tuned": best.best}
-    for path, over in (("batched", best.best), ("plain", {})):
+    # the tuner also chooses the dice grid (8x8 or 16x16), scored by micropolygons/s
+    best = autotune.tune(sc, frames=3, warmup=1, use_cache=False, tune_patch_size=True)
+    rates = {}
+    for t in best.trials:
+        ps = t.options.get("reyes_patch_size", 8)
+        rates[ps] = max(rates.get(ps, 0.0), t.micropolygons / (t.ms / 1e3))
+    out = {"patches": sc.n_patches, "views": 64, "tuned": best.best,
+           "best_rate_by_dice_grid": {f"{k}x{k}": v for k, v in sorted(rates.items())}}
+    ps = {"reyes_patch_size": best.best.get("reyes_patch_size", 8)}
+    for path, over in (("batched", best.best), ("plain", ps)):
         r = renderer_for(sc, path, **over)
         r.set_stream(stream.cuda_stream)
         render_scene(r, sc)
@@ -483,7 +546,8 @@ def main():
     frame_s = t_dev / args.steps
     frame_bytes = cp_alg + S * 20 + W * H * (8 + 8 + 16)
     roofline = {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak_gbs, "unit": "GB/s",
-                "frac": achieved / peak_gbs, "traffic": NCU_TRAFFIC.get(dominant), "peak_kind": peak_kind,
+                "frac": achieved / peak_gbs, "traffic": ncu_figure(dominant, "traffic"),
+                "traffic_source": source_hash(dominant), "peak_kind": peak_kind,
                 "stage_ms": stage_ms, "alg_bytes": dom_bytes,
                 "atomic": {"kernel": "dice_raster", "achieved": atom_rate, "peak": atom_peak["tiled"],
                            "peak_random": atom_peak["random"], "unit": "atomicMin/s",
@@ -495,10 +559,11 @@ def main():
     sms = torch.cuda.get_device_properties(dev).multi_processor_count
     clk = clk.summary()
     mhz = clk.get("sm_mhz") or clk.get("sm_max_mhz") or 0
-    if dominant in NCU_INST and mhz and dom_s > 0:
+    inst = ncu_figure(dominant, "inst")
+    if inst and mhz and dom_s > 0:
         peak_issue = sms * 4 * mhz * 1e6
-        roofline["issue"] = {"kernel": dominant, "achieved": NCU_INST[dominant] / dom_s, "peak": peak_issue,
-                             "unit": "warp instructions/s", "frac": NCU_INST[dominant] / dom_s / peak_issue,
+        roofline["issue"] = {"kernel": dominant, "achieved": inst / dom_s, "peak": peak_issue,
+                             "unit": "warp instructions/s", "frac": inst / dom_s / peak_issue,
                              "sms": sms, "sm_mhz": mhz}
 
     extras = {}
@@ -530,24 +595,38 @@ def main():
         pst = rp.stats()
         plain_ms = statistics.mean(pms)
         extras["plain"] = {"ms_per_frame": plain_ms, "value": pst["micropolygons"] / (plain_ms / 1e3),
-                           "passes": pst["passes"], "micropolygons": pst["micropolygons"]}
+                           "passes": pst["passes"], "micropolygons": pst["micropolygons"],
+                           **plain_grid_bytes(8, pst["subpatches"], plain_ms)}
         extras["batched_over_plain"] = value / extras["plain"]["value"]
         rp.close()
-        # backward / forward on the displaced 16x16 heightfield at 512x512
-        try:
-            from micropolis_gb300 import adjoint
-            extras["adjoint"] = adjoint.bench_bwd_fwd(stream)
-        except Exception as e:  # noqa: BLE001
-            extras["adjoint"] = {"error": str(e)[:200]}
+        # backward / forward on the displaced heightfields: 16x16 patches at
+        # 512x512 and 512x512 patches at 3840x2160
+        from micropolis_gb300 import adjoint
+        for key, wl, n in (("adjoint", "heightfield16_512x512", 10), ("adjoint_4k", "heightfield512_3840x2160", 5)):
+            try:
+                extras[key] = adjoint.bench_bwd_fwd(stream, steps=n, workload=wl)
+            except Exception as e:  # noqa: BLE001
+                extras[key] = {"error": str(e)[:200]}
+        # depth complexity of the same frame with backface culling off
+        rb = renderer_for(sc, "batched", backface_culling=0)
+        rb.set_stream(stream.cuda_stream)
+        for h, d in zip(handles, sc.draws):
+            rb.load_patches(h, d.mesh.cp, d.mesh.type)
+        rb.prepare()
+        for h, d in zip(handles, sc.draws):
+            rb.draw_patches(h, d.mv, proj, d.color)
+        rb.finish()
+        _, dep_nb = rb.read_framebuffer()
+        nb_frags = rb.stats()["fragments"]
+        extras["no_backface_culling"] = {"fragments": nb_frags, "fragments_per_pixel": nb_frags / (W * H),
+                                         "depth_complexity_covered":
+                                             nb_frags / max(int(np.count_nonzero(dep_nb != 0x7FFFFFFF)), 1)}
+        rb.close()
         extras["views64"] = views64_leg(stream)
-        # CPU baseline: bounded sample on the host cores
+        # CPU baseline: whole frames on the host cores, the same definition as --impl reference
         cores = os.cpu_count() or 1
-        per = 4096      # every process renders the whole frame: about 10-15 s of CPU work each
         with cpu_pool(cores) as pool:
-            cv, cmp, cwall, cbusy = cpu_baseline(WORKLOAD, cores, per, pool)
-        extras["cpu_baseline"] = {"value": cv, "unit": "micropolygons/s", "cores": cores, "kind": "port",
-                                  "sample": f"{cores} processes, each bound&split+dice+shade+sample of {per} of "
-                                            f"the 4096 patches ({cmp} micropolygons in {cbusy:.1f} s)"}
+            extras["cpu_baseline"] = cpu_baseline_line(WORKLOAD, pool, cores, frames=5)
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "micropolygons/s", "n_gpus": world,

@@ -116,8 +116,38 @@ def bench_bwd_fwd(stream=None, steps: int = 10, workload: str = "heightfield16_5
             frame.append(dr.r.stats()["gpu_ms"])
         del loss
     f, bk, fr = float(np.median(fwd)), float(np.median(bwd)), float(np.median(frame))
+    work = backward_work(sc, dr.r)
     # fwd_ms: the autograd forward as a caller sees it (control-point
     # widening and upload, amplitude copy, the frame, the image copy);
     # frame_ms: the batched frame alone (device time of its graph)
     return {"workload": f"{workload} (displacement on)", "fwd_ms": f, "frame_ms": fr, "bwd_ms": bk,
-            "bwd_over_fwd": bk / f, "bwd_over_frame": bk / fr}
+            "bwd_over_fwd": bk / f, "bwd_over_frame": bk / fr, **work,
+            "bwd_gbs": work["B_bwd"] / (bk / 1e3) / 1e9, "bwd_updates_per_s": work["A_bwd"] / (bk / 1e3)}
+
+
+def backward_work(scene, r, view: int = 0) -> dict:
+    """Algorithmic work of one backward pass over the last frame of r:
+    B_bwd = W*H*(8 + 16 + 16) B (the depth|id key, dL/dcolour and the
+    colour of every pixel) + 12 B per control point of the gradient;
+    A_bwd = control-point gradient updates the adjoint kernel issues (one
+    per control-point coordinate per warp of 32 pixels when every pixel of
+    the warp has the same winning patch, else one per covered pixel;
+    updates of zero are skipped on the device, so this is an upper bound)."""
+    import numpy as np
+    W, H = scene.width, scene.height
+    ncp = sum(d.mesh.n_patches * d.mesh.cp.shape[1] for d in scene.draws)
+    vis = r.visibility(view)
+    draw, pid, _ = r.subpatches()
+    PS2 = r.options.reyes_patch_size ** 2
+    covered = vis >= 0
+    owner = np.full(len(vis), -1, np.int64)
+    s = vis[covered] // PS2
+    owner[covered] = (draw[s].astype(np.int64) << 32) | pid[s].astype(np.int64)
+    per = np.zeros(len(vis), np.int64)
+    cps = np.array([d.mesh.cp.shape[1] for d in scene.draws])
+    per[covered] = cps[draw[s]] * 3
+    n = len(vis) // 32 * 32
+    wo = owner[:n].reshape(-1, 32)
+    uniform = np.all(wo == wo[:, :1], axis=1) & (wo[:, 0] >= 0)
+    a = int(per[:n].reshape(-1, 32)[~uniform].sum() + per[:n].reshape(-1, 32)[uniform, 0].sum() + per[n:].sum())
+    return {"B_bwd": W * H * 40 + 12 * ncp, "A_bwd": a, "covered_pixels": int(covered.sum())}

@@ -53,6 +53,7 @@ __device__ __forceinline__ void bns_reset(unsigned long long* ctrl, long long ro
     *cw(ctrl, kBigOverflow) = 0;
     *cw(ctrl, kGroupTicket) = 0;
     *cw(ctrl, kMaxDepth) = 0;
+    *cw(ctrl, kSortDone) = 0;
 }
 
 __device__ __forceinline__ void set_status(unsigned long long* ctrl, int code) {

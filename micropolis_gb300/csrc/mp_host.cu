@@ -1109,13 +1109,18 @@ mp_status mp_dump_trace(mp_ctx* c, char* buf, size_t cap) {
     if (c->trace.empty())
         return fail(c, MP_ERR_STATE,
                     "the plain path times its commands only with stage timing on (mp_set_stage_timing)");
+    long long prev_end = 0;
     for (size_t i = 0; i < c->trace.size(); ++i) {
         const auto& e = c->trace[i];
-        // each command depends on the one before it on the stream
-        bool ok = i == 0 ? put(buf, cap, &pos, "%s@%s:%lld:%lld:%lld:%lld:%zu:\n", e.name, queue, e.start, e.start,
-                               e.start, e.end, i)
-                         : put(buf, cap, &pos, "%s@%s:%lld:%lld:%lld:%lld:%zu:%zu\n", e.name, queue, e.start, e.start,
-                               e.start, e.end, i, i - 1);
+        // each command depends on the one before it on the stream, so it
+        // starts no earlier than that one ends (event times are rounded to
+        // the nanosecond independently)
+        const long long start = std::max(e.start, prev_end), end = std::max(e.end, start);
+        prev_end = end;
+        bool ok = i == 0 ? put(buf, cap, &pos, "%s@%s:%lld:%lld:%lld:%lld:%zu:\n", e.name, queue, start, start,
+                               start, end, i)
+                         : put(buf, cap, &pos, "%s@%s:%lld:%lld:%lld:%lld:%zu:%zu\n", e.name, queue, start, start,
+                               start, end, i, i - 1);
         if (!ok) return MP_ERR_OVERFLOW;
     }
     return MP_OK;

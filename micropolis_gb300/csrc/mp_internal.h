@@ -29,7 +29,9 @@ enum CtrlWord {
     kGroupTicket,      // sub-patch groups claimed by the frame kernel's rasterizers
     kMaxDepth,         // deepest split path of an emitted sub-patch (canonical sort keys)
     kSortTicket,       // tile tickets of the canonical sort, one word per radix pass (kSortPasses)
-    kNumCtrl = kSortTicket + 8
+    kSortPlan = kSortTicket + 8,   // what each radix pass does this frame, one word per pass (mp_sort.cu)
+    kSortDone = kSortPlan + 8,     // blocks of the sort's count kernel that have added their counts
+    kNumCtrl
 };
 constexpr int kCtrlStride = 16;  // unsigned long long words per line
 

@@ -22,16 +22,19 @@
 // radix sort).  A pass splits the keys into tiles of kSortTile, one per
 // resident block at a time (rounds of gridDim.x tiles): each tile ranks its
 // digits stably (per-warp counters; lanes with equal digits found by one
-// ballot per digit bit), publishes its digit counts, reorders itself by
+// warp match), publishes its digit counts, reorders itself by
 // digit in shared memory while it waits until every tile of its round and
 // the earlier ones has published, adds up the counts of the tiles before it
 // (independent loads, no chain of waits), and writes each digit's run of
 // the tile to consecutive addresses.  The first pass that moves keys forms
 // them from the records; the last writes the sub-patch records themselves
 // in canonical order.
-//   keys  -- digit counts of every pass;
+//   keys  -- digit counts of every pass; the block that adds the last counts
+//            writes the frame's plan: which passes move keys (a digit that is
+//            the same for every key moves nothing), which of them is first
+//            and last, and the key width;
 //   pass  -- one launch per digit position the frame's keys can have; a pass
-//            whose digit is the same for every key returns at once.
+//            the plan skips returns after reading its plan word.
 // Every wait is bounded (MP_ERR_TIMEOUT, no write after it).
 #include "mp_bns_loop.cuh"
 
@@ -74,18 +77,10 @@ __device__ __forceinline__ unsigned long long pack_key(unsigned root, unsigned p
     return D == 0 ? (unsigned long long)root : ((unsigned long long)root << D) | (path >> (32u - D));
 }
 
-// Lanes of the warp whose 8-bit digit equals this lane's (one ballot per
-// bit; valid = false lanes form a group of their own).
+// Lanes of the warp whose 8-bit digit equals this lane's (valid = false
+// lanes form a group of their own).
 __device__ __forceinline__ unsigned match_digit(unsigned d, bool valid) {
-    unsigned peers = __ballot_sync(0xffffffffu, valid);
-    if (!valid) peers = ~peers;
-#pragma unroll
-    for (int b = 0; b < 8; ++b) {
-        const unsigned bit = (d >> b) & 1u;
-        const unsigned m = __ballot_sync(0xffffffffu, bit);
-        peers &= bit ? m : ~m;
-    }
-    return peers;
+    return __match_any_sync(0xffffffffu, valid ? d : 0x100u);
 }
 
 // Bits of the frame's keys: the root bits of its root count above D path bits.
@@ -98,10 +93,19 @@ __device__ __forceinline__ int key_bits(const unsigned long long* ctrl, unsigned
     return root_bits + (int)D;
 }
 
+// Plan word of one pass (ctrl kSortPlan + pass).
+constexpr unsigned long long kPlanMoves = 1ull;          // the pass moves keys
+constexpr unsigned long long kPlanLast = 1ull << 1;      // ... and is the last that does: it writes the records
+constexpr unsigned long long kPlanWide = 1ull << 2;      // 64-bit keys (else 32-bit)
+constexpr unsigned long long kPlanCopy = 1ull << 3;      // no pass moves: this one copies the records as they are
+__device__ __forceinline__ int plan_moves_before(unsigned long long w) { return (int)((w >> 8) & 0xffu); }
+__device__ __forceinline__ unsigned plan_depth(unsigned long long w) { return (unsigned)(w >> 32); }
+
 // Digit counts of the passes the frame's keys reach (warp-aggregated: one
 // shared add per distinct digit of a warp's 32 keys); clears the next
 // frame's counts, this frame's tile-group counts and its published-tile
-// counters.
+// counters.  The last block to add its counts writes the plan of the
+// frame's passes.
 __global__ void __launch_bounds__(kKeysBlock) sort_keys_kernel(const int* __restrict__ root_prefix, SubPatches in,
                                                                SortBuffers sb, unsigned long long* ctrl,
                                                                int n_passes) {
@@ -120,7 +124,7 @@ __global__ void __launch_bounds__(kKeysBlock) sort_keys_kernel(const int* __rest
     const int active = (bits + 7) / 8 < n_passes ? (bits + 7) / 8 : n_passes;
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
-    // whole warps step together so that the ballots below see every lane
+    // whole warps step together so that the warp matches below see every lane
     for (long long base = (long long)blockIdx.x * kKeysBlock + (threadIdx.x & ~31); base < n; base += gstride) {
         const long long i = base + lane;
         const bool valid = i < n;
@@ -140,6 +144,38 @@ __global__ void __launch_bounds__(kKeysBlock) sort_keys_kernel(const int* __rest
     for (int i = threadIdx.x; i < active * kDigits; i += kKeysBlock) {
         const unsigned v = (&s_hist[0][0])[i];
         if (v) atomicAdd(hist + i, v);
+    }
+    __threadfence();
+    __shared__ int s_last;
+    __syncthreads();
+    if (threadIdx.x == 0) s_last = atomicAdd(ctrl + kSortDone * kCtrlStride, 1ull) == gridDim.x - 1;
+    __syncthreads();
+    if (!s_last) return;
+    // the last block: every count is in; a pass moves keys unless one digit holds them all
+    __threadfence();
+    const int tid = threadIdx.x, warp = tid >> 5;
+    __shared__ int s_same[kSortPasses];
+    if (tid < kSortPasses) s_same[tid] = 0;
+    __syncthreads();
+    if (tid < kDigits)
+        for (int p = 0; p < active; ++p)
+            if ((long long)__ldcg(hist + p * kDigits + tid) == n) s_same[p] = 1;   // (at most one digit can)
+    __syncthreads();
+    if (warp == 0 && lane == 0) {
+        int moving = 0;
+        for (int p = 0; p < active; ++p) moving += s_same[p] ? 0 : 1;
+        int before = 0, seen = 0;
+        for (int p = 0; p < n_passes; ++p) {
+            unsigned long long w = ((unsigned long long)D << 32) | (bits > 32 ? kPlanWide : 0ull) |
+                                   ((unsigned long long)before << 8);
+            if (p < active && !s_same[p]) {
+                w |= kPlanMoves;
+                if (++seen == moving) w |= kPlanLast;
+                ++before;
+            }
+            if (moving == 0 && p == n_passes - 1) w |= kPlanCopy;
+            ctrl[(kSortPlan + p) * kCtrlStride] = w;
+        }
     }
 }
 
@@ -326,20 +362,43 @@ __device__ __forceinline__ void pass_body(PassSmem& sm, const int* __restrict__ 
             __syncthreads();
         }
         // each digit's run of the tile to consecutive addresses
-        for (int j = tid; j < tn; j += kSortBlock) {
-            const K key = skeys[j];
-            const unsigned d = digit_of(key, pass);
-            const long long dst = (long long)sm.base[d] + (j - (int)sm.tstart[d]);
-            if (dst < n) {
-                const unsigned sv = sm.vals[j];
-                if (last) {
-                    if (dst < out.capacity && sv < (unsigned)n) {
-                        out.range[dst] = __ldcg(in.range + sv);
-                        out.meta[dst] = __ldcg(in.meta + sv);
+        if (last) {
+            // the records, gathered two at a time with their loads issued together
+            constexpr int kBatch = 2;
+            for (int j0 = tid; j0 < tn; j0 += kBatch * kSortBlock) {
+                float4 rg[kBatch];
+                int2 mt[kBatch];
+                long long dst[kBatch];
+#pragma unroll
+                for (int u = 0; u < kBatch; ++u) {
+                    const int j = j0 + u * kSortBlock;
+                    dst[u] = -1;
+                    if (j < tn) {
+                        const unsigned d = digit_of(skeys[j], pass);
+                        const long long o = (long long)sm.base[d] + (j - (int)sm.tstart[d]);
+                        const unsigned sv = sm.vals[j];
+                        if (o < n && o < out.capacity && sv < (unsigned)n) {
+                            dst[u] = o;
+                            rg[u] = __ldcg(in.range + sv);
+                            mt[u] = __ldcg(in.meta + sv);
+                        }
                     }
-                } else {
+                }
+#pragma unroll
+                for (int u = 0; u < kBatch; ++u)
+                    if (dst[u] >= 0) {
+                        out.range[dst[u]] = rg[u];
+                        out.meta[dst[u]] = mt[u];
+                    }
+            }
+        } else {
+            for (int j = tid; j < tn; j += kSortBlock) {
+                const K key = skeys[j];
+                const unsigned d = digit_of(key, pass);
+                const long long dst = (long long)sm.base[d] + (j - (int)sm.tstart[d]);
+                if (dst < n) {
                     kout[dst] = key;
-                    vout[dst] = sv;
+                    vout[dst] = sm.vals[j];
                 }
             }
         }
@@ -360,46 +419,31 @@ __global__ void __launch_bounds__(kSortBlock, 2) sort_pass_kernel(const int* __r
     extern __shared__ __align__(16) unsigned char smem_raw[];
     PassSmem& sm = *reinterpret_cast<PassSmem*>(smem_raw);
     const int tid = threadIdx.x;
-    const long long n = sort_count(ctrl, in, sb);
-    const unsigned* hist = hist_of(sb, frame_epoch(ctrl));
-    unsigned D = 0;
-    const int bits = key_bits(ctrl, &D);
-    const int active = (bits + 7) / 8 < n_passes ? (bits + 7) / 8 : n_passes;
-    // passes that move keys: those within the keys' bits whose digit is not
-    // the same for every key (the counts of all passes are loaded first)
-    unsigned h[kSortPasses];
-#pragma unroll
-    for (int q = 0; q < kSortPasses; ++q) h[q] = q < active && tid < kDigits ? hist[q * kDigits + tid] : 0u;
-    int moves_before = 0, moves_after = 0;
-    bool moves = false;
-    unsigned h_pass = 0;
-#pragma unroll
-    for (int q = 0; q < kSortPasses; ++q) {
-        if (q >= active) break;
-        const int same = __syncthreads_or(tid < kDigits && (long long)h[q] == n);
-        if (q == pass) h_pass = h[q];
-        if (!same) {
-            if (q < pass) ++moves_before;
-            else if (q == pass) moves = true;
-            else ++moves_after;
+    // written by the frame's earlier launches: plain loads, issued together
+    const unsigned long long plan = __ldcg(ctrl + (kSortPlan + pass) * kCtrlStride);
+    long long n = (long long)__ldcg(ctrl + kOutCount * kCtrlStride);
+    const unsigned epoch = (unsigned)__ldcg(ctrl + kEpoch * kCtrlStride);
+    if (n > in.capacity) n = in.capacity;
+    if (n > sb.capacity) n = sb.capacity;
+    if (plan & kPlanCopy) {
+        // no pass moves anything (n <= 1): the records are already in order
+        const long long stride = (long long)gridDim.x * kSortBlock;
+        for (long long j = (long long)blockIdx.x * kSortBlock + tid; j < n && j < out.capacity; j += stride) {
+            out.range[j] = in.range[j];
+            out.meta[j] = in.meta[j];
         }
-    }
-    const long long stride = (long long)gridDim.x * kSortBlock;
-    if (!moves) {
-        // no pass moved anything (n <= 1): the records are already in order
-        if (pass == n_passes - 1 && moves_before == 0)
-            for (long long j = (long long)blockIdx.x * kSortBlock + tid; j < n && j < out.capacity; j += stride) {
-                out.range[j] = in.range[j];
-                out.meta[j] = in.meta[j];
-            }
         return;
     }
-    const bool last = moves_after == 0;
-    if (bits <= 32)
-        pass_body<unsigned>(sm, root_prefix, in, out, sb, ctrl, pass, n, D, moves_before, last, h_pass, spin_limit);
-    else
-        pass_body<unsigned long long>(sm, root_prefix, in, out, sb, ctrl, pass, n, D, moves_before, last, h_pass,
+    if (!(plan & kPlanMoves)) return;
+    const unsigned h_pass = tid < kDigits ? __ldcg(hist_of(sb, epoch) + pass * kDigits + tid) : 0u;
+    const unsigned D = plan_depth(plan);
+    const int before = plan_moves_before(plan);
+    const bool last = (plan & kPlanLast) != 0;
+    if (plan & kPlanWide)
+        pass_body<unsigned long long>(sm, root_prefix, in, out, sb, ctrl, pass, n, D, before, last, h_pass,
                                       spin_limit);
+    else
+        pass_body<unsigned>(sm, root_prefix, in, out, sb, ctrl, pass, n, D, before, last, h_pass, spin_limit);
 }
 
 int sm_count() {

@@ -78,3 +78,22 @@ def test_trace_and_stats_formats(built, cuda, path):
             r.dump_trace()
         assert e.value.status == _lib.MP_ERR_STATE
     r.close()
+
+
+@pytest.mark.parametrize("path", ["batched", "plain"])
+def test_trace_matches_committed_fixture(built, cuda, path):
+    """The trace fixture that tests/test_trace_tools_cpu.py feeds to the
+    reference's own tools still has the form this library writes: the same
+    commands in the same order, ids and dependencies for the same frame."""
+    import os
+    import sys
+    from oracle import oracle
+    here = os.path.dirname(os.path.abspath(__file__))
+    sys.path.insert(0, os.path.join(here, "golden"))
+    import make_trace_fixtures
+    trace, _ = make_trace_fixtures.frame_texts(path)
+    live = oracle.parse_trace(trace)
+    with open(os.path.join(here, "golden", f"trace_{path}.txt")) as f:
+        fixture = oracle.parse_trace(f.read())
+    assert [(it[0], it[1], it[6], it[7]) for it in live] == [(it[0], it[1], it[6], it[7]) for it in fixture]
+    assert all(b[4] >= a[5] for a, b in zip(live, live[1:]))

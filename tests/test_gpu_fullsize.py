@@ -67,10 +67,14 @@ def test_mixed4096_full_size(built, cuda):
     assert len(got) == len(pb)                      # no duplicates
     assert got == subpatch_set(pp, gp, dp)
     want = set()
+    bounds = 0
     for k in range(2):
-        pid, rng, _ = oracle.bound_n_split(sc, k)
+        pid, rng, nb = oracle.bound_n_split(sc, k)
         want |= subpatch_set(pid, rng, np.full(len(pid), k))
+        bounds += nb
     assert got == want
+    # every range bounded once, as by the oracle's bound-and-split
+    assert rb.stats()["bounds"] == bounds
     assert _dyadic_ok(gb)
     assert rb.stats()["micropolygons"] == 64 * len(pb)
     assert rb.stats()["fragments"] == rp.stats()["fragments"]
