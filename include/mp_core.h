@@ -195,6 +195,21 @@ mp_status mp_framebuffer(mp_ctx* ctx, void** color_dev, void** depth_dev, int32_
 /* Copies layer `view` to host memory; linear != 0 converts to row-major (y up). */
 mp_status mp_read_framebuffer(mp_ctx* ctx, int32_t view, float* color_rgba, int32_t* depth, int32_t linear);
 
+/* Read-back of layer `view` (tiled colour float4, depth int32) that overlaps
+ * the frames rendered after it: the layer is copied on the device into a
+ * staging layer of the context (on the context's stream, after the frame),
+ * then to `color` / `depth` in host memory on a copy stream of its own, and
+ * the call returns at once.  The host buffers should be page-locked
+ * (cudaMallocHost / cudaHostRegister) for the copy to run asynchronously;
+ * either pointer may be NULL.  mp_wait_read_framebuffer returns when the last
+ * requested read-back is in host memory; the host buffers must not be read
+ * or reused before then.  A new request first waits, on the device, until the
+ * previous one has left the staging layer.  The first call allocates the
+ * staging layer (20 bytes per pixel) and the copy stream.  The reference
+ * reads its framebuffer back synchronously (src/Reyes/Framebuffer.cpp:102-124). */
+mp_status mp_read_framebuffer_async(mp_ctx* ctx, int32_t view, float* color_rgba, int32_t* depth);
+mp_status mp_wait_read_framebuffer(mp_ctx* ctx);
+
 /* Copies layer `view` (tiled colour float4, depth int32) into device buffers on
  * the context's stream; either pointer may be NULL. */
 mp_status mp_copy_framebuffer_device(mp_ctx* ctx, int32_t view, void* color_dev, void* depth_dev);

@@ -81,6 +81,8 @@ SIGNATURES = [
     ("mp_backward", ctypes.c_int, [c_void_p, i32, c_void_p, c_void_p]),
     ("mp_set_displacement_amplitude", ctypes.c_int, [c_void_p, f32]),
     ("mp_set_displacement_amplitude_device", ctypes.c_int, [c_void_p, c_void_p]),
+    ("mp_read_framebuffer_async", ctypes.c_int, [c_void_p, i32, c_void_p, c_void_p]),
+    ("mp_wait_read_framebuffer", ctypes.c_int, [c_void_p]),
     ("mp_update_patches_device", ctypes.c_int, [c_void_p, u64, c_void_p]),
     ("mp_inclusive_scan", ctypes.c_int, [c_void_p, P(i32), P(i32), i64]),
     ("mp_inclusive_scan_noalloc", ctypes.c_int, [c_void_p, c_void_p, i64, c_void_p]),

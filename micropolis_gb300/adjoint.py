@@ -28,36 +28,66 @@ class DiffRenderer:
         self.proj = Projection(scene.fovy, scene.near, (scene.width, scene.height))
         self.r.load_patches(handle, d.mesh.cp, d.mesh.type)
         self.npx = scene.width * scene.height
+        self._side = None
 
-    def _bind_stream(self):
-        self.r.set_stream(torch.cuda.current_stream().cuda_stream)
+    def _stream_in(self):
+        """Binds the renderer to the stream of a call made on torch's
+        current stream: that stream itself, or -- for the legacy default
+        stream, on which a frame's CUDA graph cannot be captured -- a side
+        stream that first waits for it.  Returns (caller's stream, side
+        stream or None) for _stream_out."""
+        cur = torch.cuda.current_stream()
+        if cur.cuda_stream != 0:
+            self.r.set_stream(cur.cuda_stream)
+            return cur, None
+        if self._side is None:
+            self._side = torch.cuda.Stream(device=cur.device)
+        self._side.wait_stream(cur)
+        self.r.set_stream(self._side.cuda_stream)
+        return cur, self._side
+
+    @staticmethod
+    def _stream_out(cur, side, *tensors):
+        """The caller's stream waits for the side stream's work on `tensors`."""
+        if side is not None:
+            for t in tensors:
+                t.record_stream(side)
+            cur.wait_stream(side)
 
     def render(self, cp: torch.Tensor, amp) -> torch.Tensor:
         """Tiled RGBA image (W*H, 4) for control points cp (n, per, 3) and
         the displacement amplitude multiplier amp: a tensor on the device
         (read there, no host synchronization) or a number."""
-        self._bind_stream()
         xyz1 = torch.cat([cp.detach().float().reshape(-1, 3),
                           torch.ones(cp.numel() // 3, 1, device=cp.device)], dim=1).contiguous()
-        self.r.update_patches_device(self.handle, xyz1.data_ptr())
+        amp_dev = None
         if isinstance(amp, torch.Tensor):
-            self._amp = amp.detach().to(device=cp.device, dtype=torch.float32).reshape(1).contiguous()
-            self.r.set_displacement_amplitude_device(self._amp.data_ptr())
+            amp_dev = amp.detach().to(device=cp.device, dtype=torch.float32).reshape(1).contiguous()
+        img = torch.empty((self.npx, 4), dtype=torch.float32, device=cp.device)
+        cur, side = self._stream_in()
+        self.r.update_patches_device(self.handle, xyz1.data_ptr())
+        if amp_dev is not None:
+            self.r.set_displacement_amplitude_device(amp_dev.data_ptr())
         else:
             self.r.set_displacement_amplitude(float(amp))
         self.r.prepare()
         self.r.draw_patches(self.handle, self.draw.mv, self.proj, self.draw.color)
         self.r.finish()
-        img = torch.empty((self.npx, 4), dtype=torch.float32, device=cp.device)
         self.r.copy_framebuffer_device(0, img.data_ptr())
+        self._stream_out(cur, side, img, xyz1, *([amp_dev] if amp_dev is not None else []))
         return img
 
     def backward(self, grad_img: torch.Tensor, cp_shape, device):
-        self._bind_stream()
-        g_cp = torch.zeros(int(torch.tensor(cp_shape).prod().item()), dtype=torch.float32, device=device)
+        n = 1
+        for k in cp_shape:
+            n *= int(k)
+        g_cp = torch.zeros(n, dtype=torch.float32, device=device)
         g_amp = torch.zeros(1, dtype=torch.float32, device=device)
+        g_img = grad_img.contiguous()
+        cur, side = self._stream_in()
         self.r.set_grad_buffer(0, g_cp.data_ptr())
-        self.r.backward(0, grad_img.contiguous().data_ptr(), g_amp.data_ptr())
+        self.r.backward(0, g_img.data_ptr(), g_amp.data_ptr())
+        self._stream_out(cur, side, g_cp, g_amp, g_img)
         return g_cp.reshape(cp_shape), g_amp
 
 
@@ -84,9 +114,18 @@ def bench_bwd_fwd(stream=None, steps: int = 10, workload: str = "heightfield16_5
     """Forward (frame) and backward (adjoint) device times on a displaced
     heightfield workload (default the 16x16 one at 512x512) with an L2 image
     loss against a target rendered from perturbed control points: N(0, 0.05)
-    for 16 x 16 patches, scaled with the patch spacing for finer grids."""
+    for 16 x 16 patches, scaled with the patch spacing for finer grids.  Runs
+    on `stream` (a torch stream; None: the current stream), with CUDA events
+    on that stream around the autograd forward and the backward."""
+    import contextlib
     import numpy as np
     from . import scenes
+    ctx = torch.cuda.stream(stream) if stream is not None else contextlib.nullcontext()
+    with ctx:
+        return _bench_bwd_fwd(steps, workload, np, scenes)
+
+
+def _bench_bwd_fwd(steps, workload, np, scenes) -> dict:
     sc = scenes.WORKLOADS[workload]()
     dev = torch.device("cuda")
     dr = DiffRenderer(sc)

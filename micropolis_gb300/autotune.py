@@ -10,7 +10,10 @@ not the rendered sub-patch set:
 - ``raster_tile``: the tile edge, in pixels, of the depth|id key buffer that
   the 64-bit atomicMin resolves visibility in (8, 16 or 32);
 - ``overlap``: bound-and-split and rasterization in one launch, with the
-  rasterizing blocks consuming sub-patches as they are emitted, or in two;
+  rasterizing blocks consuming sub-patches as they are emitted, or separate
+  launches with the canonical sub-patch order between them.  The overlapped
+  form numbers micropolygons in emission order, so its depth-tie winners
+  depend on scheduling; it is a candidate only with ``allow_overlap``;
 - optionally ``reyes_patch_size`` (the dice grid, 8 or 16).  The dice grid
   sets how many micropolygons each sub-patch makes, so the image changes with
   it; it is tuned only when asked for, and the score is then micropolygons
@@ -34,7 +37,7 @@ from typing import Callable, Dict, Iterable, List, Optional
 GROUPS = {8: (8, 11, 16, 22), 16: (2, 3, 4, 6)}
 DEFAULT_GROUP = {8: 11, 16: 6}   # the library's default dice_group per dice grid
 TILES = (8, 16, 32)
-OVERLAP = (False, True)
+OVERLAP = (False, True)       # the values tried with allow_overlap
 CACHE_VERSION = 1
 
 
@@ -182,20 +185,22 @@ def device_name() -> str:
     return ""
 
 
-def tune(scene, frames: int = 5, warmup: int = 2, tune_patch_size: bool = False, cache: Optional[str] = None,
+def tune(scene, frames: int = 5, warmup: int = 2, tune_patch_size: bool = False, allow_overlap: bool = False,
+         cache: Optional[str] = None,
          use_cache: bool = True, space: Optional[List[dict]] = None,
          measure: Optional[Callable[[object, dict, int, int], Trial]] = None, device: Optional[str] = None) -> Result:
     """Times every candidate on `scene` and returns (and caches) the fastest."""
     ps = int(scene.options.get("reyes_patch_size", 8))
     dev = device_name() if device is None else device
-    key = signature(scene, None, dev) + ("+ps" if tune_patch_size else "")
+    key = signature(scene, None, dev) + ("+ps" if tune_patch_size else "") + ("+overlap" if allow_overlap else "")
     data = load_cache(cache) if use_cache else {"version": CACHE_VERSION}
     if use_cache and key in data:
         e = data[key]
         return Result(key, dict(e["best"]), [Trial(dict(t["options"]), t["ms"], t["micropolygons"])
                                             for t in e.get("trials", [])], cached=True)
     measure = measure or measure_batched
-    space = space if space is not None else candidates(ps, tune_patch_size)
+    space = space if space is not None else candidates(ps, tune_patch_size,
+                                                       overlap=OVERLAP if allow_overlap else (False,))
     trials = [measure(scene, c, frames, warmup) for c in space]
     best = choose(trials, by_rate=tune_patch_size)
     if use_cache:

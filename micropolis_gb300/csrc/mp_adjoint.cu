@@ -84,9 +84,12 @@ __device__ __forceinline__ void vertex_forward(const DrawDev& d, const FrameDev&
     }
 }
 
-constexpr int kAdjBlock = 256;
+// 128-thread blocks, three per SM within the register file (about 160
+// registers a thread): 12 warps per SM where 256-thread blocks fit only one
+// block (8 warps).
+constexpr int kAdjBlock = 128;
 
-__global__ void __launch_bounds__(kAdjBlock) adjoint_kernel(const DrawDev* __restrict__ draws, FrameDev frp,
+__global__ void __launch_bounds__(kAdjBlock, 3) adjoint_kernel(const DrawDev* __restrict__ draws, FrameDev frp,
                                                             SubPatches sub, Framebuffer fb,
                                                             const float4* __restrict__ grad_color, float* grad_amp,
                                                             int view) {

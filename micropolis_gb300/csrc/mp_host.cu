@@ -116,6 +116,12 @@ struct mp_ctx {
     unsigned char* image = nullptr;   // device buffer of mp_read_image
     long long image_bytes = 0;
     float* d_amp = nullptr;           // displacement amplitude multiplier read by the displacing kernels
+    // asynchronous read-back: a device copy of one layer, sent to the host on its own stream
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t ev_staged = nullptr, ev_copied = nullptr;
+    float4* stage_color = nullptr;
+    int* stage_depth = nullptr;
+    bool readback_pending = false;
 };
 
 namespace {
@@ -815,6 +821,14 @@ mp_status mp_create(const mp_options* opts, mp_ctx** out) {
 void mp_destroy(mp_ctx* c) {
     if (!c) return;
     if (c->stream) cudaStreamSynchronize(c->stream);
+    if (c->copy_stream) {
+        cudaStreamSynchronize(c->copy_stream);
+        cudaStreamDestroy(c->copy_stream);
+    }
+    if (c->ev_staged) cudaEventDestroy(c->ev_staged);
+    if (c->ev_copied) cudaEventDestroy(c->ev_copied);
+    dfree(c->stage_color);
+    dfree(c->stage_depth);
     invalidate_graph(c);
     for (auto& kv : c->meshes) dfree(kv.second.cp);
     dfree(c->ctrl);
@@ -1214,6 +1228,47 @@ mp_status mp_read_framebuffer(mp_ctx* c, int32_t view, float* color, int32_t* de
     if (ddst) CK(cudaMemcpyAsync(ddst, c->fb.depth + view * n, sizeof(int) * (size_t)n, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     if (linear) untile(cdst, ddst, color, depth, c->fr.W, c->fr.H);
+    return MP_OK;
+}
+
+mp_status mp_read_framebuffer_async(mp_ctx* c, int32_t view, float* color, int32_t* depth) {
+    if (!c || view < 0 || view >= c->fb.views || (!color && !depth)) return MP_ERR_INVALID_ARG;
+    if (!c->frame_valid) return fail(c, MP_ERR_STATE, "no finished frame");
+    if (c->in_frame) return fail(c, MP_ERR_STATE, "read-back inside a frame");
+    const long long n = c->fb.pixels;
+    if (!c->copy_stream) {
+        // first use: the staging layer, a copy stream and its events
+        CK(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+        CK(cudaEventCreateWithFlags(&c->ev_staged, cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&c->ev_copied, cudaEventDisableTiming));
+        CK(dalloc(&c->stage_color, n));
+        CK(dalloc(&c->stage_depth, n));
+    }
+    // the staging layer is free once the previous read-back has left it
+    if (c->readback_pending) CK(cudaStreamWaitEvent(c->stream, c->ev_copied, 0));
+    if (color)
+        CK(cudaMemcpyAsync(c->stage_color, c->fb.color + view * n, sizeof(float4) * (size_t)n,
+                           cudaMemcpyDeviceToDevice, c->stream));
+    if (depth)
+        CK(cudaMemcpyAsync(c->stage_depth, c->fb.depth + view * n, sizeof(int) * (size_t)n,
+                           cudaMemcpyDeviceToDevice, c->stream));
+    CK(cudaEventRecord(c->ev_staged, c->stream));
+    CK(cudaStreamWaitEvent(c->copy_stream, c->ev_staged, 0));
+    if (color)
+        CK(cudaMemcpyAsync(color, c->stage_color, sizeof(float4) * (size_t)n, cudaMemcpyDeviceToHost,
+                           c->copy_stream));
+    if (depth)
+        CK(cudaMemcpyAsync(depth, c->stage_depth, sizeof(int) * (size_t)n, cudaMemcpyDeviceToHost, c->copy_stream));
+    CK(cudaEventRecord(c->ev_copied, c->copy_stream));
+    c->readback_pending = true;
+    return MP_OK;
+}
+
+mp_status mp_wait_read_framebuffer(mp_ctx* c) {
+    if (!c) return MP_ERR_INVALID_ARG;
+    if (!c->readback_pending) return MP_OK;
+    CK(cudaEventSynchronize(c->ev_copied));
+    c->readback_pending = false;
     return MP_OK;
 }
 

@@ -246,6 +246,16 @@ class Renderer:
                                           _f32p(dep)))
         return pos, pxl, dep
 
+    def read_framebuffer_async(self, view: int, color_ptr: int, depth_ptr: int) -> None:
+        """Starts the read-back of layer `view` into host buffers (tiled
+        float4 colour, int32 depth; page-locked for an asynchronous copy) and
+        returns at once; wait_read_framebuffer() completes it."""
+        self._ck(lib().mp_read_framebuffer_async(self._ctx, view, ctypes.c_void_p(color_ptr or None),
+                                                 ctypes.c_void_p(depth_ptr or None)))
+
+    def wait_read_framebuffer(self) -> None:
+        self._ck(lib().mp_wait_read_framebuffer(self._ctx))
+
     def set_displacement_amplitude(self, amp: float) -> None:
         self._ck(lib().mp_set_displacement_amplitude(self._ctx, float(amp)))
 

@@ -97,3 +97,33 @@ def test_trace_matches_committed_fixture(built, cuda, path):
         fixture = oracle.parse_trace(f.read())
     assert [(it[0], it[1], it[6], it[7]) for it in live] == [(it[0], it[1], it[6], it[7]) for it in fixture]
     assert all(b[4] >= a[5] for a, b in zip(live, live[1:]))
+
+
+def test_async_read_back_equals_sync(built, cuda):
+    """mp_read_framebuffer_async: frames read back while the next frame
+    renders equal the synchronous read-back of each frame, bit for bit, with
+    two alternating host buffers and a different camera every frame."""
+    torch = cuda
+    from micropolis_gb300 import scenes
+    from micropolis_gb300.renderer import render_scene, renderer_for
+    base = _scene()
+    r = renderer_for(base, "batched")
+    n = base.width * base.height
+    cols = [torch.empty((n, 4), dtype=torch.float32).pin_memory().numpy() for _ in range(2)]
+    deps = [torch.empty((n,), dtype=torch.int32).pin_memory().numpy() for _ in range(2)]
+    want = []
+    for k in range(4):
+        sc = scenes.mixed4096_1920x1080(n=256, width=640, height=448, distance=11.0 + k)
+        render_scene(r, sc)
+        c, d = r.read_framebuffer()
+        want.append((c.copy(), d.copy()))
+        if k >= 2:
+            # the buffers of frame k - 2 are reused: its read-back must have landed
+            assert np.array_equal(deps[k % 2], want[k - 2][1])
+        r.read_framebuffer_async(0, cols[k % 2].ctypes.data, deps[k % 2].ctypes.data)
+        if k % 2 == 1:
+            r.wait_read_framebuffer()
+            for j in (k - 1, k):
+                assert np.array_equal(deps[j % 2], want[j][1])
+                assert np.array_equal(cols[j % 2].view(np.uint32), want[j][0].view(np.uint32))
+    r.close()

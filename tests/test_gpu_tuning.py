@@ -81,7 +81,8 @@ def test_autotuner_on_gpu(built, cuda, tmp_path):
     sc = _scene(8)
     cache = str(tmp_path / "tune.json")
     res = autotune.tune(sc, frames=2, warmup=1, cache=cache)
-    assert len(res.trials) == 24 and all(t.ms > 0 for t in res.trials)
+    assert len(res.trials) == 12 and all(t.ms > 0 for t in res.trials)
+    assert not any(t.options["overlap"] for t in res.trials)
     assert len({t.micropolygons for t in res.trials}) == 1
     assert autotune.tune(sc, cache=cache).cached
     r = autotune.tuned_renderer(sc, cache=cache)
