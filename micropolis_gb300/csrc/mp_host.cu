@@ -470,9 +470,9 @@ const SubPatches& final_list(const mp_ctx* c) {
 
 // Kernel launches of one batched frame.
 long long batched_kernels(const mp_ctx* c) {
-    // clear+reset, (bound-and-split, sort keys, sort passes, dice+raster | overlapped), slow raster, resolve
+    // clear+reset, (bound-and-split, canonical sort, dice+raster | overlapped), slow raster, resolve
     if (overlapped(c)) return 4;
-    return 5 + 1 + c->sort_passes;
+    return 6;
 }
 
 void launch_sort(mp_ctx* c) {

@@ -29,8 +29,7 @@ enum CtrlWord {
     kGroupTicket,      // sub-patch groups claimed by the frame kernel's rasterizers
     kMaxDepth,         // deepest split path of an emitted sub-patch (canonical sort keys)
     kSortTicket,       // tile tickets of the canonical sort, one word per radix pass (kSortPasses)
-    kSortPlan = kSortTicket + 8,   // what each radix pass does this frame, one word per pass (mp_sort.cu)
-    kSortDone = kSortPlan + 8,     // blocks of the sort's count kernel that have added their counts
+    kSortDone = kSortTicket + 8,   // grid-barrier arrivals of the sort kernel this frame
     kNumCtrl
 };
 constexpr int kCtrlStride = 16;  // unsigned long long words per line
@@ -111,13 +110,13 @@ long long scan_state_words(long long n);
 long long sort_tiles(long long n);
 // Sorts the n_out (device count kOutCount) sub-patches of `in` by (root,
 // path) and gathers them into `out`; root_prefix as for bound-and-split.
-// Launches the radix passes of digits [0, n_passes) (a pass whose digit is
-// the same for every key of the frame returns at once).
+// One launch; the keys have at most n_passes 8-bit digits (a pass whose digit
+// is the same for every key of the frame is skipped).
 void launch_canonical_sort(const int* root_prefix, const SubPatches& in, const SubPatches& out, const SortBuffers& sb,
                            unsigned long long* ctrl, long long spin_limit, int n_passes, int resident_grid,
                            cudaStream_t s);
-// Blocks of the sort's pass kernel resident at once (also sets its shared
-// memory size; call outside stream capture).
+// Blocks of the sort kernel resident at once (also sets its shared memory
+// size; call outside stream capture).
 int canonical_sort_grid();
 // The radix passes the keys of a frame can need: root bits up to `roots`
 // above at most min(32, max_split_depth + 1) path bits.

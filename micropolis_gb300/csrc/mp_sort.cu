@@ -17,24 +17,24 @@
 // key that packs the root above the frame's D path bits (D = the deepest
 // emitted sub-patch, which bound-and-split records; below bit 32 - D every
 // path is zero, so the order is that of (root << 32 | path)).  Keys are 32
-// bits wide when the frame's root and path bits fit, else 64.  Digit counts
-// of every pass are taken once, up front (Adinets & Merrill's one-sweep
-// radix sort).  A pass splits the keys into tiles of kSortTile, one per
-// resident block at a time (rounds of gridDim.x tiles): each tile ranks its
-// digits stably (per-warp counters; lanes with equal digits found by one
-// warp match), publishes its digit counts, reorders itself by
-// digit in shared memory while it waits until every tile of its round and
-// the earlier ones has published, adds up the counts of the tiles before it
-// (independent loads, no chain of waits), and writes each digit's run of
-// the tile to consecutive addresses.  The first pass that moves keys forms
-// them from the records; the last writes the sub-patch records themselves
-// in canonical order.
-//   keys  -- digit counts of every pass; the block that adds the last counts
-//            writes the frame's plan: which passes move keys (a digit that is
-//            the same for every key moves nothing), which of them is first
-//            and last, and the key width;
-//   pass  -- one launch per digit position the frame's keys can have; a pass
-//            the plan skips returns after reading its plan word.
+// bits wide when the frame's root and path bits fit, else 64.  It is one
+// launch of a resident grid, in phases separated by grid barriers (bounded
+// waits on a counter of the frame's control words):
+//   counts -- the digit counts of every pass at once (Adinets & Merrill's
+//             one-sweep radix sort; warp matches aggregate a warp's equal
+//             digits into one shared add), added to the frame's table;
+//   plan   -- every block reads the table: a pass whose digit is the same
+//             for every key moves nothing and is skipped;
+//   passes -- each moving pass splits the keys into tiles of kSortTile, one
+//             per block at a time (rounds of gridDim.x tiles): each tile
+//             ranks its digits stably (per-warp counters, warp matches),
+//             publishes its digit counts, reorders itself by digit in shared
+//             memory while it waits until every tile of its round and the
+//             earlier ones has published, adds up the counts of the tiles
+//             before it (independent loads, no chain of waits), and writes
+//             each digit's run of the tile to consecutive addresses.  The
+//             first moving pass forms the keys from the records; the last
+//             writes the sub-patch records themselves in canonical order.
 // Every wait is bounded (MP_ERR_TIMEOUT, no write after it).
 #include "mp_bns_loop.cuh"
 
@@ -93,90 +93,32 @@ __device__ __forceinline__ int key_bits(const unsigned long long* ctrl, unsigned
     return root_bits + (int)D;
 }
 
-// Plan word of one pass (ctrl kSortPlan + pass).
-constexpr unsigned long long kPlanMoves = 1ull;          // the pass moves keys
-constexpr unsigned long long kPlanLast = 1ull << 1;      // ... and is the last that does: it writes the records
-constexpr unsigned long long kPlanWide = 1ull << 2;      // 64-bit keys (else 32-bit)
-constexpr unsigned long long kPlanCopy = 1ull << 3;      // no pass moves: this one copies the records as they are
-__device__ __forceinline__ int plan_moves_before(unsigned long long w) { return (int)((w >> 8) & 0xffu); }
-__device__ __forceinline__ unsigned plan_depth(unsigned long long w) { return (unsigned)(w >> 32); }
-
-// Digit counts of the passes the frame's keys reach (warp-aggregated: one
-// shared add per distinct digit of a warp's 32 keys); clears the next
-// frame's counts, this frame's tile-group counts and its published-tile
-// counters.  The last block to add its counts writes the plan of the
-// frame's passes.
-__global__ void __launch_bounds__(kKeysBlock) sort_keys_kernel(const int* __restrict__ root_prefix, SubPatches in,
-                                                               SortBuffers sb, unsigned long long* ctrl,
-                                                               int n_passes) {
-    __shared__ unsigned s_hist[kSortPasses][kDigits];
-    for (int i = threadIdx.x; i < kSortPasses * kDigits; i += kKeysBlock) (&s_hist[0][0])[i] = 0;
-    const unsigned epoch = frame_epoch(ctrl);
-    unsigned* next = hist_of(sb, epoch + 1);
-    const long long gt = (long long)blockIdx.x * kKeysBlock + threadIdx.x, gstride = (long long)gridDim.x * kKeysBlock;
-    for (long long i = gt; i < kSortPasses * kDigits; i += gstride) next[i] = 0;
-    for (long long i = gt; i < kSortPasses * sb.groups * kDigits; i += gstride) sb.group_counts[i] = 0;
-    if (blockIdx.x == 0 && threadIdx.x < kSortPasses) ctrl[(kSortTicket + threadIdx.x) * kCtrlStride] = 0;
+// Waits (bounded) until every block of the grid has arrived at barrier
+// number `k` of the frame (the counter ctrl kSortDone is zeroed by the
+// frame's reset); false when the wait ran out (the status is then set).
+__device__ __forceinline__ bool grid_barrier(unsigned long long* ctrl, unsigned long long k, long long spin_limit,
+                                             int* s_flag) {
     __syncthreads();
-    const long long n = sort_count(ctrl, in, sb);
-    unsigned D = 0;
-    const int bits = key_bits(ctrl, &D);
-    const int active = (bits + 7) / 8 < n_passes ? (bits + 7) / 8 : n_passes;
-    const int lane = threadIdx.x & 31;
-    const unsigned lt = (1u << lane) - 1u;
-    // whole warps step together so that the warp matches below see every lane
-    for (long long base = (long long)blockIdx.x * kKeysBlock + (threadIdx.x & ~31); base < n; base += gstride) {
-        const long long i = base + lane;
-        const bool valid = i < n;
-        unsigned long long key = 0;
-        if (valid) {
-            const int2 m = in.meta[i];
-            key = pack_key((unsigned)(__ldg(root_prefix + m.y) + m.x), in.path[i], D);
-        }
-        for (int p = 0; p < active; ++p) {
-            const unsigned d = digit_of(key, p);
-            const unsigned peers = match_digit(d, valid);
-            if (valid && (peers & lt) == 0) atomicAdd(&s_hist[p][d], (unsigned)__popc(peers));
-        }
-    }
-    __syncthreads();
-    unsigned* hist = hist_of(sb, epoch);
-    for (int i = threadIdx.x; i < active * kDigits; i += kKeysBlock) {
-        const unsigned v = (&s_hist[0][0])[i];
-        if (v) atomicAdd(hist + i, v);
-    }
-    __threadfence();
-    __shared__ int s_last;
-    __syncthreads();
-    if (threadIdx.x == 0) s_last = atomicAdd(ctrl + kSortDone * kCtrlStride, 1ull) == gridDim.x - 1;
-    __syncthreads();
-    if (!s_last) return;
-    // the last block: every count is in; a pass moves keys unless one digit holds them all
-    __threadfence();
-    const int tid = threadIdx.x, warp = tid >> 5;
-    __shared__ int s_same[kSortPasses];
-    if (tid < kSortPasses) s_same[tid] = 0;
-    __syncthreads();
-    if (tid < kDigits)
-        for (int p = 0; p < active; ++p)
-            if ((long long)__ldcg(hist + p * kDigits + tid) == n) s_same[p] = 1;   // (at most one digit can)
-    __syncthreads();
-    if (warp == 0 && lane == 0) {
-        int moving = 0;
-        for (int p = 0; p < active; ++p) moving += s_same[p] ? 0 : 1;
-        int before = 0, seen = 0;
-        for (int p = 0; p < n_passes; ++p) {
-            unsigned long long w = ((unsigned long long)D << 32) | (bits > 32 ? kPlanWide : 0ull) |
-                                   ((unsigned long long)before << 8);
-            if (p < active && !s_same[p]) {
-                w |= kPlanMoves;
-                if (++seen == moving) w |= kPlanLast;
-                ++before;
+    if (threadIdx.x == 0) {
+        unsigned long long* ctr = ctrl + kSortDone * kCtrlStride;
+        __threadfence();
+        atomicAdd(ctr, 1ull);
+        const unsigned long long need = k * gridDim.x;
+        long long spins = 0;
+        int ok = 1;
+        while (ld_acquire_u64(ctr) < need) {
+            if (++spins > spin_limit) {
+                ok = 0;
+                set_status(ctrl, kErrTimeout);
+                break;
             }
-            if (moving == 0 && p == n_passes - 1) w |= kPlanCopy;
-            ctrl[(kSortPlan + p) * kCtrlStride] = w;
+            __nanosleep(32);
         }
+        __threadfence();
+        *s_flag = ok;
     }
+    __syncthreads();
+    return *s_flag != 0;
 }
 
 // Shared memory of one pass block (the 64-bit layout; 32-bit keys use the
@@ -214,11 +156,11 @@ __device__ __forceinline__ unsigned scan_digits(unsigned v, unsigned* warp_sum) 
     return before + x - v;
 }
 
-// One moving pass over keys of type K (see sort_pass_kernel).
+// One moving pass over keys of type K (see sort_kernel).
 //   from_records -- the first moving pass: keys formed from the records
 //   last         -- the last moving pass: records written in key order
 template <typename K>
-__device__ __forceinline__ void pass_body(PassSmem& sm, const int* __restrict__ root_prefix, const SubPatches& in,
+__device__ __forceinline__ bool pass_body(PassSmem& sm, const int* __restrict__ root_prefix, const SubPatches& in,
                                           const SubPatches& out, const SortBuffers& sb, unsigned long long* ctrl,
                                           int pass, long long n, unsigned D, int moves_before, bool last,
                                           unsigned h_pass, long long spin_limit) {
@@ -330,7 +272,7 @@ __device__ __forceinline__ void pass_body(PassSmem& sm, const int* __restrict__ 
         if (sm.fail) {
             // a wait ran out: report it and write nothing with a wrong base
             if (tid == 0) set_status(ctrl, kErrTimeout);
-            return;
+            return false;
         }
         {
             // counts of the earlier tiles, digit d: thread d adds the whole
@@ -404,28 +346,76 @@ __device__ __forceinline__ void pass_body(PassSmem& sm, const int* __restrict__ 
         }
         __syncthreads();
     }
+    return true;
 }
 
-// One radix pass.  Tile t (kSortTile keys) is block t % gridDim.x's, in
-// round t / gridDim.x; the grid is resident, and every block publishes its
-// tile's digit counts before it waits, so the waits end.  A tile's start in
-// digit bin d is the bin's start plus the counts of the earlier tiles, read
-// as the sums of whole groups of kSortGroup tiles (accumulated as tiles
-// publish) and the single counts of its own group's earlier tiles.
-__global__ void __launch_bounds__(kSortBlock, 2) sort_pass_kernel(const int* __restrict__ root_prefix, SubPatches in,
-                                                                  SubPatches out, SortBuffers sb,
-                                                                  unsigned long long* ctrl, int pass, int n_passes,
-                                                                  long long spin_limit) {
+// The whole sort in one launch of a resident grid (see the file header).
+// A tile's start in digit bin d is the bin's start plus the counts of the
+// earlier tiles, read as the sums of whole groups of kSortGroup tiles
+// (accumulated as tiles publish) and the single counts of its own group's
+// earlier tiles.
+__global__ void __launch_bounds__(kSortBlock, 2) sort_kernel(const int* __restrict__ root_prefix, SubPatches in,
+                                                             SubPatches out, SortBuffers sb, unsigned long long* ctrl,
+                                                             int n_passes, long long spin_limit) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     PassSmem& sm = *reinterpret_cast<PassSmem*>(smem_raw);
-    const int tid = threadIdx.x;
-    // written by the frame's earlier launches: plain loads, issued together
-    const unsigned long long plan = __ldcg(ctrl + (kSortPlan + pass) * kCtrlStride);
-    long long n = (long long)__ldcg(ctrl + kOutCount * kCtrlStride);
-    const unsigned epoch = (unsigned)__ldcg(ctrl + kEpoch * kCtrlStride);
-    if (n > in.capacity) n = in.capacity;
-    if (n > sb.capacity) n = sb.capacity;
-    if (plan & kPlanCopy) {
+    __shared__ int s_flag;
+    const int tid = threadIdx.x, lane = tid & 31;
+    const long long n = sort_count(ctrl, in, sb);
+    const unsigned epoch = frame_epoch(ctrl);
+    unsigned D = 0;
+    const int bits = key_bits(ctrl, &D);
+    const int active = (bits + 7) / 8 < n_passes ? (bits + 7) / 8 : n_passes;
+    unsigned* hist = hist_of(sb, epoch);
+    {
+        // counts: of this block's stripe of keys into shared memory (the
+        // front of the pass buffers), then into the frame's table; the next
+        // frame's table, the group counts and the passes' published-tile
+        // counters are cleared for later
+        unsigned* s_hist = reinterpret_cast<unsigned*>(smem_raw);
+        for (int i = tid; i < kSortPasses * kDigits; i += kSortBlock) s_hist[i] = 0;
+        unsigned* next = hist_of(sb, epoch + 1);
+        const long long gt = (long long)blockIdx.x * kSortBlock + tid, gstride = (long long)gridDim.x * kSortBlock;
+        for (long long i = gt; i < kSortPasses * kDigits; i += gstride) next[i] = 0;
+        for (long long i = gt; i < kSortPasses * sb.groups * kDigits; i += gstride) sb.group_counts[i] = 0;
+        if (blockIdx.x == 0 && tid < kSortPasses) ctrl[(kSortTicket + tid) * kCtrlStride] = 0;
+        __syncthreads();
+        const unsigned lt = (1u << lane) - 1u;
+        // whole warps step together so that the warp matches below see every lane
+        for (long long base = (long long)blockIdx.x * kSortBlock + (tid & ~31); base < n; base += gstride) {
+            const long long i = base + lane;
+            const bool valid = i < n;
+            unsigned long long key = 0;
+            if (valid) {
+                const int2 m = __ldcg(in.meta + i);
+                key = pack_key((unsigned)(__ldg(root_prefix + m.y) + m.x), __ldcg(in.path + i), D);
+            }
+            for (int p = 0; p < active; ++p) {
+                const unsigned d = digit_of(key, p);
+                const unsigned peers = match_digit(d, valid);
+                if (valid && (peers & lt) == 0) atomicAdd(&s_hist[p * kDigits + d], (unsigned)__popc(peers));
+            }
+        }
+        __syncthreads();
+        for (int i = tid; i < active * kDigits; i += kSortBlock) {
+            const unsigned v = s_hist[i];
+            if (v) atomicAdd(hist + i, v);
+        }
+    }
+    unsigned long long barrier = 0;
+    if (!grid_barrier(ctrl, ++barrier, spin_limit, &s_flag)) return;
+    // plan: a pass moves keys unless one digit holds them all
+    int moving = 0;
+    unsigned moves_mask = 0;
+#pragma unroll 1
+    for (int q = 0; q < active; ++q) {
+        const unsigned hq = tid < kDigits ? __ldcg(hist + q * kDigits + tid) : 0u;
+        if (!__syncthreads_or(tid < kDigits && (long long)hq == n)) {
+            moves_mask |= 1u << q;
+            ++moving;
+        }
+    }
+    if (moving == 0) {
         // no pass moves anything (n <= 1): the records are already in order
         const long long stride = (long long)gridDim.x * kSortBlock;
         for (long long j = (long long)blockIdx.x * kSortBlock + tid; j < n && j < out.capacity; j += stride) {
@@ -434,16 +424,23 @@ __global__ void __launch_bounds__(kSortBlock, 2) sort_pass_kernel(const int* __r
         }
         return;
     }
-    if (!(plan & kPlanMoves)) return;
-    const unsigned h_pass = tid < kDigits ? __ldcg(hist_of(sb, epoch) + pass * kDigits + tid) : 0u;
-    const unsigned D = plan_depth(plan);
-    const int before = plan_moves_before(plan);
-    const bool last = (plan & kPlanLast) != 0;
-    if (plan & kPlanWide)
-        pass_body<unsigned long long>(sm, root_prefix, in, out, sb, ctrl, pass, n, D, before, last, h_pass,
-                                      spin_limit);
-    else
-        pass_body<unsigned>(sm, root_prefix, in, out, sb, ctrl, pass, n, D, before, last, h_pass, spin_limit);
+    int before = 0;
+#pragma unroll 1
+    for (int q = 0; q < active; ++q) {
+        if (!((moves_mask >> q) & 1u)) continue;
+        const unsigned hq = tid < kDigits ? __ldcg(hist + q * kDigits + tid) : 0u;   // thread d: count of digit d
+        const bool last = before == moving - 1;
+        bool ok;
+        if (bits <= 32)
+            ok = pass_body<unsigned>(sm, root_prefix, in, out, sb, ctrl, q, n, D, before, last, hq, spin_limit);
+        else
+            ok = pass_body<unsigned long long>(sm, root_prefix, in, out, sb, ctrl, q, n, D, before, last, hq,
+                                               spin_limit);
+        if (!ok) return;
+        // the next pass reads what every block of this one wrote
+        if (!last && !grid_barrier(ctrl, ++barrier, spin_limit, &s_flag)) return;
+        ++before;
+    }
 }
 
 int sm_count() {
@@ -467,22 +464,19 @@ int canonical_sort_passes(int max_split_depth, long long roots) {
 }
 
 int canonical_sort_grid() {
-    // blocks resident at once (the passes' waits rely on it)
-    cudaFuncSetAttribute(sort_pass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(PassSmem));
+    // blocks resident at once (the grid barriers and round waits rely on it)
+    cudaFuncSetAttribute(sort_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(PassSmem));
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sort_pass_kernel, kSortBlock, sizeof(PassSmem));
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sort_kernel, kSortBlock, sizeof(PassSmem));
     return sm_count() * (per_sm < 1 ? 1 : per_sm);
 }
 
 void launch_canonical_sort(const int* root_prefix, const SubPatches& in, const SubPatches& out, const SortBuffers& sb,
                            unsigned long long* ctrl, long long spin_limit, int n_passes, int resident_grid,
                            cudaStream_t s) {
-    sort_keys_kernel<<<sm_count(), kKeysBlock, 0, s>>>(root_prefix, in, sb, ctrl, n_passes);
     const long long tiles = sb.tiles < 1 ? 1 : sb.tiles;
     const int grid = (int)(tiles < resident_grid ? tiles : resident_grid);
-    for (int p = 0; p < n_passes; ++p)
-        sort_pass_kernel<<<grid, kSortBlock, sizeof(PassSmem), s>>>(root_prefix, in, out, sb, ctrl, p, n_passes,
-                                                                    spin_limit);
+    sort_kernel<<<grid, kSortBlock, sizeof(PassSmem), s>>>(root_prefix, in, out, sb, ctrl, n_passes, spin_limit);
 }
 
 }  // namespace mp

@@ -118,13 +118,3 @@ def assert_identical_to_oracle(r, scene, params=None, oracle_frame=None):
     st = r.stats()
     assert st["micropolygons"] == ost["micropolygons"] and st["fragments"] == ost["fragments"]
     return ost
-
-
-def sort_passes(max_split_depth, roots):
-    """Radix passes the batched frame launches for its canonical order: 8-bit
-    digits of root bits (up to roots - 1) above at most min(32,
-    max_split_depth + 1) path bits."""
-    path_bits = min(32, max_split_depth + 1)
-    root_bits = int(roots - 1).bit_length() if roots > 1 else 0
-    bits = path_bits + root_bits
-    return 1 if bits <= 8 else (bits + 7) // 8

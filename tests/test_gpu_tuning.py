@@ -4,7 +4,7 @@ sub-patch set, fragment count and image as the oracle."""
 import numpy as np
 import pytest
 
-from helpers import assert_identical_to_oracle, framebuffer_diff, sort_passes, subpatch_set
+from helpers import assert_identical_to_oracle, framebuffer_diff, subpatch_set
 
 pytestmark = pytest.mark.gpu
 
@@ -41,7 +41,6 @@ def test_knobs_match_oracle(built, cuda, ps, groups):
     sc = _scene(ps)
     want, ocol, odep, ost = _oracle(sc)
     frame = oracle.render(sc, params=oracle.make_params(sc), want_win=True)
-    passes = sort_passes(23, sc.n_patches)
     for tile in (8, 16, 32):
         for group in groups:
             for overlap in (False, True):
@@ -49,8 +48,8 @@ def test_knobs_match_oracle(built, cuda, ps, groups):
                 render_scene(r, sc)
                 if not overlap:
                     assert_identical_to_oracle(r, sc, oracle.make_params(sc), frame)
-                    # clear, bound-and-split, sort keys, sort passes, dice+raster, slow raster, resolve
-                    assert r.stats()["kernels"] == 6 + passes
+                    # clear, bound-and-split, canonical sort, dice+raster, slow raster, resolve
+                    assert r.stats()["kernels"] == 6
                     r.close()
                     continue
                 d, p, g = r.subpatches()
