@@ -22,6 +22,44 @@ __device__ __forceinline__ float bern(int i, float t) {
     return i == 0 ? s * s * s : i == 1 ? 3.0f * s * s * t : i == 2 ? 3.0f * s * t * t : t * t * t;
 }
 
+// Effective weight of every control point at (tx, ty) (the dice evaluators).
+__device__ __forceinline__ int cp_weights(int type, float tx, float ty, float* w) {
+    if (type == 0) {
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) w[4 * i + j] = bern(i, tx) * bern(j, ty);
+        return 16;
+    }
+#pragma unroll
+    for (int k = 0; k < 20; ++k) w[k] = 0.0f;
+    float u = tx, v = ty;
+    auto bl = [](float a, float b, float den, float& wa, float& wb) {
+        wa = a / den;
+        wb = b / den;
+        if (!isfinite(wa) || !isfinite(wb)) { wa = 0.0f; wb = 0.0f; }
+    };
+    float a0, b0, a1, b1, a2, b2, a3, b3;
+    bl(u, v, u + v, a0, b0);                       // F0 = (u P12 + v P16) / (u + v)
+    bl(1.0f - u, v, 1.0f - u + v, a1, b1);         // F1 = ((1-u) P17 + v P13) / (1 - u + v)
+    bl(1.0f - u, 1.0f - v, 2.0f - u - v, a2, b2);  // F2 = ((1-u) P14 + (1-v) P18) / (2 - u - v)
+    bl(u, 1.0f - v, 1.0f + u - v, a3, b3);         // F3 = (u P19 + (1-v) P15) / (1 + u - v)
+    const int slot[16] = {0, 4, 9, 1, 8, -1, -2, 5, 7, -4, -3, 10, 3, 11, 6, 2};
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            float b = bern(i, tx) * bern(j, ty);
+            int sl = slot[4 * i + j];
+            if (sl >= 0) w[sl] += b;
+            else if (sl == -1) { w[12] += b * a0; w[16] += b * b0; }
+            else if (sl == -2) { w[17] += b * a1; w[13] += b * b1; }
+            else if (sl == -3) { w[14] += b * a2; w[18] += b * b2; }
+            else { w[19] += b * a3; w[15] += b * b3; }
+        }
+    return 20;
+}
+
 struct VertexTrace {
     float x[4], y[4], z[4];   // eye position before each displacement step and after the last
 };
@@ -158,71 +196,36 @@ __global__ void __launch_bounds__(kAdjBlock, 3) adjoint_kernel(const DrawDev* __
     long long key = active ? ((long long)draw << 32) | (unsigned)pid : -1;
     unsigned peers = __match_any_sync(0xffffffffu, key);
     bool uniform = __all_sync(0xffffffffu, peers == 0xffffffffu) && key != -1;
-    if (!uniform && !active) return;
-    // Each Bernstein term (i, j) of the four vertices feeds one control point
-    // (a Gregory face-blend term two, with the blend weights): its gradient
-    // is sum_k w_k * go(vertex k), the same products and order as a table of
-    // the 16 or 20 weights per vertex would give, computed term by term so
-    // that no per-vertex table lives in local memory.
-    float bu[4][4], bv[4][4];
+    float wv[4][20];
+    int nw = ncp;
+    if (active) {
 #pragma unroll
-    for (int k = 0; k < 4; ++k)
+        for (int k = 0; k < 4; ++k) nw = cp_weights(dp->type, tx4[k], ty4[k], wv[k]);
+    }
+    if (uniform) {
+        // every lane holds the same patch: reduce each coordinate across the warp
+        float* g = dp->grad_cp + (size_t)pid * nw * 3;
+        for (int j = 0; j < nw; ++j)
 #pragma unroll
-        for (int i = 0; i < 4; ++i) {
-            bu[k][i] = bern(i, tx4[k]);
-            bv[k][i] = bern(i, ty4[k]);
-        }
-    const bool greg = dp->type != 0;
-    float* g = dp->grad_cp + (size_t)pid * ncp * 3;
-    auto emit = [&](int slot, const float* w) {
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-            float v = w[0] * go_acc[0][c] + w[1] * go_acc[1][c] + w[2] * go_acc[2][c] + w[3] * go_acc[3][c];
-            if (uniform) {
-                // every lane holds the same patch: reduce each coordinate across the warp
+            for (int c = 0; c < 3; ++c) {
+                float v = wv[0][j] * go_acc[0][c] + wv[1][j] * go_acc[1][c] + wv[2][j] * go_acc[2][c] +
+                          wv[3][j] * go_acc[3][c];
                 v += __shfl_xor_sync(0xffffffffu, v, 16);
                 v += __shfl_xor_sync(0xffffffffu, v, 8);
                 v += __shfl_xor_sync(0xffffffffu, v, 4);
                 v += __shfl_xor_sync(0xffffffffu, v, 2);
                 v += __shfl_xor_sync(0xffffffffu, v, 1);
-                if (lane == 0 && v != 0.0f) atomicAdd(g + 3 * slot + c, v);
-            } else if (v != 0.0f) {
-                atomicAdd(g + 3 * slot + c, v);
+                if (lane == 0 && v != 0.0f) atomicAdd(g + 3 * j + c, v);
             }
-        }
-    };
-    // Gregory slot of term 4i + j, or a face blend -1..-4 (F0..F3) (the point
-    // order of the dice evaluator)
-    constexpr int kSlot[16] = {0, 4, 9, 1, 8, -1, -2, 5, 7, -4, -3, 10, 3, 11, 6, 2};
+    } else if (active) {
+        float* g = dp->grad_cp + (size_t)pid * nw * 3;
+        for (int j = 0; j < nw; ++j)
 #pragma unroll
-    for (int t = 0; t < 16; ++t) {
-        float b[4];
-#pragma unroll
-        for (int k = 0; k < 4; ++k) b[k] = bu[k][t >> 2] * bv[k][t & 3];
-        if (!greg) {
-            emit(t, b);
-        } else if (kSlot[t] >= 0) {
-            emit(kSlot[t], b);
-        } else {
-            // F = (a P_A + b P_B) / den: weights b * a / den and b * b / den (zero where the blend is 0/0)
-            const int f = -kSlot[t] - 1;
-            float wa[4], wb[4];
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                const float u = tx4[k], v = ty4[k];
-                const float a = f == 0 ? u : f == 3 ? u : 1.0f - u;
-                const float c = f == 0 ? v : f == 1 ? v : 1.0f - v;
-                const float den = f == 0 ? u + v : f == 1 ? 1.0f - u + v : f == 2 ? 2.0f - u - v : 1.0f + u - v;
-                float ra = a / den, rb = c / den;
-                if (!isfinite(ra) || !isfinite(rb)) { ra = 0.0f; rb = 0.0f; }
-                wa[k] = b[k] * ra;
-                wb[k] = b[k] * rb;
+            for (int c = 0; c < 3; ++c) {
+                float v = wv[0][j] * go_acc[0][c] + wv[1][j] * go_acc[1][c] + wv[2][j] * go_acc[2][c] +
+                          wv[3][j] * go_acc[3][c];
+                if (v != 0.0f) atomicAdd(g + 3 * j + c, v);
             }
-            // F0: P12 / P16, F1: P17 / P13, F2: P14 / P18, F3: P19 / P15
-            constexpr int kA[4] = {12, 17, 14, 19}, kB[4] = {16, 13, 18, 15};
-            emit(kA[f], wa);
-            emit(kB[f], wb);
-        }
     }
 }
 

@@ -499,6 +499,32 @@ __device__ __forceinline__ void project_vertex_m(const float* proj, const FrameD
     py = __float2int_rz(e.y);
     depth = fmul(p.z, rw);
 }
+// project_vertex_m for a glm::perspective matrix, whose only nonzero
+// entries are m0, m5, m10, m14 and m11 = -1 (the host builds every draw's
+// projection so).  For a finite position with eye z != 0 the general product
+// reduces exactly: each zero term adds a zero to a rounded product, which
+// changes at most the sign of a zero result, and the viewport transform
+// (+ W/2, + H/2) and the depth clamp do not see that sign; p.w = -z.  Any
+// other position takes the general product.
+__device__ __forceinline__ void project_vertex_persp(const float* proj, const FrameDev& fr, float4 pos, int& px,
+                                                     int& py, float& depth) {
+    const float mag = fadd(fadd(fabsf(pos.x), fabsf(pos.y)), fadd(fabsf(pos.z), fabsf(pos.w)));
+    if (!(mag < __int_as_float(0x7f800000)) || pos.z == 0.0f) {
+        project_vertex_m(proj, fr, pos, px, py, depth);
+        return;
+    }
+    const int vsx = fr.W << fr.shift, vsy = fr.H << fr.shift;
+    const float2 pxy = fmul2(make_float2(proj[0], proj[5]), make_float2(pos.x, pos.y));
+    const float pz = ffma(proj[14], pos.w, fmul(proj[10], pos.z));
+    const float rw = frcp(-pos.z);
+    float2 e = fmul2(pxy, dup2(rw));
+    e = fmul2(e, make_float2((float)vsx, (float)vsy));
+    e = fmul2(e, dup2(0.5f));
+    e = fadd2(e, make_float2((float)(vsx / 2), (float)(vsy / 2)));
+    px = __float2int_rz(e.x);
+    py = __float2int_rz(e.y);
+    depth = fmul(pz, rw);
+}
 __device__ __forceinline__ void project_vertex(const DrawDev& d, const FrameDev& fr, float4 pos, int& px, int& py,
                                                float& depth) {
     project_vertex_m(d.proj, fr, pos, px, py, depth);

@@ -313,7 +313,7 @@ __device__ __forceinline__ void raster_group(FusedSmem<PS, NS>& sm, int b, long 
                                 sm.cw[k][nv]);
         int px, py;
         float dep;
-        project_vertex_m(mvp + 16, fr, pos, px, py, dep);
+        project_vertex_persp(mvp + 16, fr, pos, px, py, dep);
         sm.pxy[i] = make_int2(px, py);
         sm.edep[i] = make_float4(pos.x, pos.y, pos.z, dep);
         if (pos.z == 0.0f) {
