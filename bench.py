@@ -50,7 +50,15 @@ KERNEL_SOURCES = {
     "resolve_or_shade": ["mp_raster.cu", "mp_device.cuh", "mp_bns_loop.cuh", "mp_internal.h"],
     "canonical_sort_or_sample": ["mp_sort.cu", "mp_bns_loop.cuh", "mp_internal.h"],
 }
-NCU_FIGURES = {}
+NCU_FIGURES = {
+    # ncu --set full of one frame (profiles/raster_fused_mixed4096_1920x1080.md and the
+    # summaries beside it), sources as of the capture
+    "dice_raster": {"source": "29884bf2bd105b71", "traffic": 101_184_768 + 66_111_744, "inst": 1_036_109_842},
+    "bound_split": {"source": "83928645e25485d2", "traffic": 2_856_960 + 213_277_696, "inst": 171_051_632},
+    "resolve_or_shade": {"source": "29884bf2bd105b71", "traffic": 61_478_400 + 6_120_448, "inst": 10_215_932},
+    "canonical_sort_or_sample": {"source": "328b0cfa8fc27777", "traffic": 30_108_928 + 6_130_432,
+                                 "inst": 33_842_919},
+}
 
 
 def source_hash(stage: str) -> str:

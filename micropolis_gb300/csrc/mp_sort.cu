@@ -26,7 +26,7 @@
 //   plan   -- every block reads the table: a pass whose digit is the same
 //             for every key moves nothing and is skipped;
 //   passes -- each moving pass splits the keys into tiles of kSortTile, one
-//             per block at a time (rounds of gridDim.x tiles): each tile
+//             per block at a time (rounds of nblk tiles): each tile
 //             ranks its digits stably (per-warp counters, warp matches),
 //             publishes its digit counts, reorders itself by digit in shared
 //             memory while it waits until every tile of its round and the
@@ -93,17 +93,17 @@ __device__ __forceinline__ int key_bits(const unsigned long long* ctrl, unsigned
     return root_bits + (int)D;
 }
 
-// Waits (bounded) until every block of the grid has arrived at barrier
+// Waits (bounded) until all nblk working blocks have arrived at barrier
 // number `k` of the frame (the counter ctrl kSortDone is zeroed by the
 // frame's reset); false when the wait ran out (the status is then set).
-__device__ __forceinline__ bool grid_barrier(unsigned long long* ctrl, unsigned long long k, long long spin_limit,
-                                             int* s_flag) {
+__device__ __forceinline__ bool grid_barrier(unsigned long long* ctrl, unsigned long long k, int nblk,
+                                             long long spin_limit, int* s_flag) {
     __syncthreads();
     if (threadIdx.x == 0) {
         unsigned long long* ctr = ctrl + kSortDone * kCtrlStride;
         __threadfence();
         atomicAdd(ctr, 1ull);
-        const unsigned long long need = k * gridDim.x;
+        const unsigned long long need = k * (unsigned long long)nblk;
         long long spins = 0;
         int ok = 1;
         while (ld_acquire_u64(ctr) < need) {
@@ -163,7 +163,7 @@ template <typename K>
 __device__ __forceinline__ bool pass_body(PassSmem& sm, const int* __restrict__ root_prefix, const SubPatches& in,
                                           const SubPatches& out, const SortBuffers& sb, unsigned long long* ctrl,
                                           int pass, long long n, unsigned D, int moves_before, bool last,
-                                          unsigned h_pass, long long spin_limit) {
+                                          unsigned h_pass, long long spin_limit, int nblk) {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const bool from_records = moves_before == 0;
     // (selects, not an indexed load: the parameter arrays stay in registers)
@@ -182,7 +182,7 @@ __device__ __forceinline__ bool pass_body(PassSmem& sm, const int* __restrict__ 
     }
     const long long n_tiles = (n + kSortTile - 1) / kSortTile;
     const unsigned lt = (1u << lane) - 1u;
-    for (long long tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
+    for (long long tile = blockIdx.x; tile < n_tiles; tile += nblk) {
         const long long t0 = tile * kSortTile;
         const int tn = (int)(n - t0 < kSortTile ? n - t0 : kSortTile);
         for (int i = tid; i < kSortWarps * kDigits; i += kSortBlock) (&sm.wcount[0][0])[i] = 0;
@@ -256,7 +256,7 @@ __device__ __forceinline__ bool pass_body(PassSmem& sm, const int* __restrict__ 
         }
         if (tid == 0) {
             // wait until every tile up to the end of this round has published
-            const long long round_end = (tile / gridDim.x + 1) * gridDim.x;
+            const long long round_end = (tile / nblk + 1) * nblk;
             const unsigned long long need = (unsigned long long)(round_end < n_tiles ? round_end : n_tiles);
             long long spins = 0;
             while (ld_acquire_u64(published) < need) {
@@ -367,6 +367,12 @@ __global__ void __launch_bounds__(kSortBlock, 2) sort_kernel(const int* __restri
     const int bits = key_bits(ctrl, &D);
     const int active = (bits + 7) / 8 < n_passes ? (bits + 7) / 8 : n_passes;
     unsigned* hist = hist_of(sb, epoch);
+    // the working blocks: one per tile of this frame's keys, at most the
+    // grid (a small frame leaves most of the resident grid idle); the others
+    // return at once and every barrier counts the working blocks only
+    const long long tiles = (n + kSortTile - 1) / kSortTile;
+    const int nblk = (int)(tiles < 1 ? 1 : tiles < gridDim.x ? tiles : gridDim.x);
+    if ((int)blockIdx.x >= nblk) return;
     {
         // counts: of this block's stripe of keys into shared memory (the
         // front of the pass buffers), then into the frame's table; the next
@@ -375,7 +381,7 @@ __global__ void __launch_bounds__(kSortBlock, 2) sort_kernel(const int* __restri
         unsigned* s_hist = reinterpret_cast<unsigned*>(smem_raw);
         for (int i = tid; i < kSortPasses * kDigits; i += kSortBlock) s_hist[i] = 0;
         unsigned* next = hist_of(sb, epoch + 1);
-        const long long gt = (long long)blockIdx.x * kSortBlock + tid, gstride = (long long)gridDim.x * kSortBlock;
+        const long long gt = (long long)blockIdx.x * kSortBlock + tid, gstride = (long long)nblk * kSortBlock;
         for (long long i = gt; i < kSortPasses * kDigits; i += gstride) next[i] = 0;
         for (long long i = gt; i < kSortPasses * sb.groups * kDigits; i += gstride) sb.group_counts[i] = 0;
         if (blockIdx.x == 0 && tid < kSortPasses) ctrl[(kSortTicket + tid) * kCtrlStride] = 0;
@@ -403,7 +409,7 @@ __global__ void __launch_bounds__(kSortBlock, 2) sort_kernel(const int* __restri
         }
     }
     unsigned long long barrier = 0;
-    if (!grid_barrier(ctrl, ++barrier, spin_limit, &s_flag)) return;
+    if (!grid_barrier(ctrl, ++barrier, nblk, spin_limit, &s_flag)) return;
     // plan: a pass moves keys unless one digit holds them all
     int moving = 0;
     unsigned moves_mask = 0;
@@ -417,7 +423,7 @@ __global__ void __launch_bounds__(kSortBlock, 2) sort_kernel(const int* __restri
     }
     if (moving == 0) {
         // no pass moves anything (n <= 1): the records are already in order
-        const long long stride = (long long)gridDim.x * kSortBlock;
+        const long long stride = (long long)nblk * kSortBlock;
         for (long long j = (long long)blockIdx.x * kSortBlock + tid; j < n && j < out.capacity; j += stride) {
             out.range[j] = in.range[j];
             out.meta[j] = in.meta[j];
@@ -432,13 +438,13 @@ __global__ void __launch_bounds__(kSortBlock, 2) sort_kernel(const int* __restri
         const bool last = before == moving - 1;
         bool ok;
         if (bits <= 32)
-            ok = pass_body<unsigned>(sm, root_prefix, in, out, sb, ctrl, q, n, D, before, last, hq, spin_limit);
+            ok = pass_body<unsigned>(sm, root_prefix, in, out, sb, ctrl, q, n, D, before, last, hq, spin_limit, nblk);
         else
             ok = pass_body<unsigned long long>(sm, root_prefix, in, out, sb, ctrl, q, n, D, before, last, hq,
-                                               spin_limit);
+                                               spin_limit, nblk);
         if (!ok) return;
         // the next pass reads what every block of this one wrote
-        if (!last && !grid_barrier(ctrl, ++barrier, spin_limit, &s_flag)) return;
+        if (!last && !grid_barrier(ctrl, ++barrier, nblk, spin_limit, &s_flag)) return;
         ++before;
     }
 }
