@@ -139,7 +139,9 @@ mp_status mp_set_stream(mp_ctx* ctx, void* stream);
 mp_status mp_are_patches_loaded(mp_ctx* ctx, uint64_t handle, int32_t* loaded);
 /* Renderer::load_patches (Renderer.h:36, PatchIndex.cpp:57-100): copies n_points xyz
  * points (16 per Bezier, 20 per Gregory patch) to the device, widened to (x,y,z,1).
- * handle is an opaque key chosen by the caller (the reference uses the mesh pointer). */
+ * handle is an opaque key chosen by the caller (the reference uses the mesh pointer).
+ * Returns once xyz has been read (the buffer may then be reused); the widening is
+ * ordered before the frames on the context's stream. */
 mp_status mp_load_patches(mp_ctx* ctx, uint64_t handle, const float* xyz, size_t n_points, mp_patch_type type);
 /* Same, from device memory (float4 x,y,z,1 per point), no host copy. */
 mp_status mp_load_patches_device(mp_ctx* ctx, uint64_t handle, const void* dev_xyz1, size_t n_points,

@@ -119,6 +119,7 @@ struct mp_ctx {
     // asynchronous read-back: a device copy of one layer, sent to the host on its own stream
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t ev_staged = nullptr, ev_copied = nullptr;
+    cudaEvent_t ev_upload = nullptr;  // end of the last host-to-device copy of patch data
     float4* stage_color = nullptr;
     int* stage_depth = nullptr;
     bool readback_pending = false;
@@ -826,6 +827,7 @@ void mp_destroy(mp_ctx* c) {
         cudaStreamDestroy(c->copy_stream);
     }
     if (c->ev_staged) cudaEventDestroy(c->ev_staged);
+    if (c->ev_upload) cudaEventDestroy(c->ev_upload);
     if (c->ev_copied) cudaEventDestroy(c->ev_copied);
     dfree(c->stage_color);
     dfree(c->stage_depth);
@@ -905,6 +907,7 @@ static mp_status load_common(mp_ctx* c, uint64_t handle, const void* src, size_t
     if (n_points) {
         if (device) {
             CK(cudaMemcpyAsync(m.cp, src, sizeof(float4) * n_points, cudaMemcpyDeviceToDevice, c->stream));
+            if (!c->in_frame) CK(cudaStreamSynchronize(c->stream));
         } else {
             // src/Reyes/PatchIndex.cpp:83-98: upload the vec3 data and widen it
             // to (x, y, z, 1) on the device.  Page-locked sources are copied
@@ -937,13 +940,17 @@ static mp_status load_common(mp_ctx* c, uint64_t handle, const void* src, size_t
                 std::memcpy(c->staging, src, bytes);
                 h = c->staging;
             }
+            if (!c->ev_upload) CK(cudaEventCreateWithFlags(&c->ev_upload, cudaEventDisableTiming));
             CK(cudaMemcpyAsync(c->xyz_dev, h, bytes, cudaMemcpyHostToDevice, c->stream));
+            CK(cudaEventRecord(c->ev_upload, c->stream));
             launch_widen_points(c->xyz_dev, m.cp, (long long)n_points, c->stream);
             CK(cudaGetLastError());
-            // the caller's page-locked buffer is read asynchronously: done before returning
-            if (pinned && c->in_frame) CK(cudaStreamSynchronize(c->stream));
+            // The call returns once the source has been read (the caller's
+            // page-locked buffer is read asynchronously; outside a frame the
+            // load is blocking like the reference's); the widening runs in
+            // stream order before any frame that reads the patches.
+            if (pinned || !c->in_frame) CK(cudaEventSynchronize(c->ev_upload));
         }
-        if (!c->in_frame) CK(cudaStreamSynchronize(c->stream));
     }
     c->meshes[handle] = m;
     return MP_OK;
