@@ -4,7 +4,12 @@ main.cpp, Scene::draw) without a window:
 
     python -m micropolis_gb300.render --workload mixed4096_1920x1080 \\
         [--path batched|plain] [--frames N] [--warmup W] [--overlap] \\
-        [--backward] [--ppm out.ppm] [--option name=value ...]
+        [--backward] [--ppm out.ppm] [--option name=value ...] \\
+        [--scene name=value ...]
+
+--scene passes arguments to the workload's generator (for instance
+n_views=8 for views64_512x512, n=256 for mixed4096_1920x1080): smaller
+instances of a workload for profiling captures.
 
 The timed frames run inside the NVTX range "frames" (a profiler's launch list
 can be filtered to them); each frame's device time (CUDA events on the
@@ -30,13 +35,18 @@ def main(argv=None) -> int:
     ap.add_argument("--backward", action="store_true", help="the adjoint pass after every frame")
     ap.add_argument("--ppm", help="write the last frame's displayed image here")
     ap.add_argument("--option", action="append", default=[], help="reyes option override, name=value")
+    ap.add_argument("--scene", action="append", default=[], help="workload generator argument, name=value")
     args = ap.parse_args(argv)
 
     import torch
     from . import scenes
     from .renderer import render_scene, renderer_for
 
-    sc = scenes.WORKLOADS[args.workload]()
+    gen = {}
+    for kv in args.scene:
+        k, _, v = kv.partition("=")
+        gen[k] = float(v) if "." in v else int(v)
+    sc = scenes.WORKLOADS[args.workload](**gen)
     over = {}
     for kv in args.option:
         k, _, v = kv.partition("=")
