@@ -91,6 +91,38 @@ def test_mixed4096_full_size(built, cuda):
     rp.close()
 
 
+def test_mixed4096_full_size_gpu_criterion(built, cuda):
+    """The headline scene under the reference's GPU bound criterion
+    (bound_criterion = 1): both paths emit the oracle's set of that
+    criterion, every range bounded once, and render the same frame."""
+    from micropolis_gb300 import scenes
+    from oracle import oracle
+    sc = scenes.mixed4096_1920x1080()
+    rb = _render(sc, "batched", bound_criterion=1)
+    rp = _render(sc, "plain", bound_criterion=1)
+    db, pb, gb = rb.subpatches()
+    dp, pp, gp = rp.subpatches()
+    got = subpatch_set(pb, gb, db)
+    assert len(got) == len(pb)
+    assert got == subpatch_set(pp, gp, dp)
+    p = oracle.make_params(sc, bound_criterion=1)
+    want = set()
+    bounds = 0
+    for k in range(len(sc.draws)):
+        pid, rng, nb = oracle.bound_n_split(sc, k, params=p)
+        want |= subpatch_set(pid, rng, np.full(len(pid), k))
+        bounds += nb
+    assert got == want
+    assert rb.stats()["bounds"] == bounds
+    assert _dyadic_ok(gb)
+    cb, zb = rb.read_framebuffer()
+    cp_, zp = rp.read_framebuffer()
+    bad, _ = framebuffer_diff(cb, zb, cp_, zp, REL_TOL)
+    assert bad <= COVERAGE_BUDGET * zb.size
+    rb.close()
+    rp.close()
+
+
 def test_mixed4096_frame_identical_to_oracle(built, cuda, pool):
     """The headline frame (4,096 mixed patches, 1920x1080, limit 8, dice
     8x8): canonical sub-patch list, colour, depth and visibility
