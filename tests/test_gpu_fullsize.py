@@ -123,16 +123,19 @@ def test_mixed4096_full_size_gpu_criterion(built, cuda):
     rp.close()
 
 
-def test_mixed4096_frame_identical_to_oracle(built, cuda, pool):
+@pytest.mark.parametrize("over", [{}, {"bound_criterion": 1}, {"reyes_patch_size": 16}],
+                         ids=["default", "gpu_criterion", "dice16"])
+def test_mixed4096_frame_identical_to_oracle(built, cuda, pool, over):
     """The headline frame (4,096 mixed patches, 1920x1080, limit 8, dice
-    8x8): canonical sub-patch list, colour, depth and visibility
+    8x8), and the same scene under the reference's GPU bound criterion and
+    at 16x16 dicing: canonical sub-patch list, colour, depth and visibility
     bit-identical to the oracle's frame at every pixel."""
     from micropolis_gb300 import scenes
     from oracle import oracle
     sc = scenes.mixed4096_1920x1080()
-    r = _render(sc, "batched")
-    frame = oracle.render_parallel(sc, pool)
-    assert_identical_to_oracle(r, sc, oracle.make_params(sc), frame)
+    r = _render(sc, "batched", **over)
+    frame = oracle.render_parallel(sc, pool, params_over=over)
+    assert_identical_to_oracle(r, sc, oracle.make_params(sc, **over), frame)
     r.close()
 
 
